@@ -1,0 +1,203 @@
+"""Python side of the G3M^3 GB300 library (ctypes over libg3m3_gpu.so).
+
+``Context`` exposes the drop-in routines with the reference's argument
+order: ``ctx.push_ion(qrho, ..., isotropic)`` takes exactly the arguments of
+sub_push_ion.f90:4-17.  Arrays may be numpy arrays (mirrored on the device,
+read back with ``ctx.sync_to_host``) or CUDA tensors (``data_ptr``).
+``Model`` drives the step engine on a device-resident multi-box state.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .params import G3M3Params, NFIELDS
+
+_vp = ctypes.c_void_p
+
+
+def addr(x):
+    """Raw address of a numpy array, CUDA tensor, ctypes object or int."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if isinstance(x, np.ndarray):
+        if not x.flags["C_CONTIGUOUS"]:
+            raise ValueError("arrays must be contiguous")
+        return x.ctypes.data
+    if hasattr(x, "data_ptr"):
+        if not x.is_contiguous():
+            raise ValueError("tensors must be contiguous")
+        return x.data_ptr()
+    if isinstance(x, ctypes.Array) or isinstance(x, ctypes.Structure):
+        return ctypes.addressof(x)
+    raise TypeError(f"cannot take the address of {type(x)}")
+
+
+class G3M3Error(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"g3m3 error {code}: {msg}")
+        self.code = code
+
+
+def table(arrays):
+    """A ctypes array of 34 addresses (the field tables of the C ABI)."""
+    t = (ctypes.c_void_p * NFIELDS)()
+    for i, a in enumerate(arrays):
+        t[i] = addr(a)
+    return t
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        self.L = _lib.load()
+        h = ctypes.c_void_p()
+        rc = self.L.g3m3_ctx_create(ctypes.byref(h), device)
+        if rc:
+            raise G3M3Error(rc, "context creation failed (no CUDA device?)")
+        self.h = h
+        self._keep = []
+
+    def close(self):
+        if self.h:
+            self.L.g3m3_ctx_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, rc):
+        if rc:
+            msg = self.L.g3m3_last_error(self.h)
+            raise G3M3Error(rc, msg.decode() if msg else "")
+        return rc
+
+    def sync_to_host(self, *arrays):
+        for a in arrays:
+            self.check(self.L.g3m3_sync_to_host(self.h, addr(a)))
+
+    def sync_to_device(self, *arrays):
+        for a in arrays:
+            self.check(self.L.g3m3_sync_to_device(self.h, addr(a)))
+
+    def synchronize(self):
+        self.check(self.L.g3m3_synchronize(self.h))
+
+    def call(self, name, *args, check=True):
+        """Call g3m3_<name>(ctx, *args); arrays are converted to addresses."""
+        fn = getattr(self.L, "g3m3_" + name)
+        conv = []
+        for a, t in zip(args, fn.argtypes[1:]):
+            if t is ctypes.c_void_p:
+                conv.append(addr(a))
+            else:
+                conv.append(a)
+        if len(conv) != len(fn.argtypes) - 1:
+            raise TypeError(f"g3m3_{name} takes {len(fn.argtypes) - 1} arguments, got {len(conv)}")
+        rc = fn(self.h, *conv)
+        return self.check(rc) if check else rc
+
+    def __getattr__(self, name):
+        if name.startswith("_") or name in ("L", "h"):
+            raise AttributeError(name)
+        return lambda *args, **kw: self.call(name, *args, **kw)
+
+
+class Model:
+    """A multi-box state on the device advanced by the step engine."""
+
+    def __init__(self, ctx: Context, state):
+        self.ctx = ctx
+        self.L = ctx.L
+        self.p = state.params
+        h = ctypes.c_void_p()
+        ctx.check(self.L.g3m3_model_create(ctx.h, ctypes.byref(self.p), ctypes.byref(h)))
+        self.h = h
+        self.upload(state)
+
+    def upload(self, state):
+        L, h = self.L, self.h
+        cur = np.ascontiguousarray(state.cur, np.float32)
+        self.ctx.check(L.g3m3_model_set_state(h, addr(cur)))
+        # the wrk copy starts as the state (wrkepres is read before written)
+        for q in range(NFIELDS):
+            self.ctx.check(L.g3m3_model_set_field(h, 2, q, addr(cur[q])))
+        b0 = np.ascontiguousarray(state.b0, np.float32)
+        self.ctx.check(L.g3m3_model_set_b0(h, addr(b0[0]), addr(b0[1]), addr(b0[2])))
+        li = state.lists
+        self._keep = [li, cur, b0]
+        rst = np.ascontiguousarray(state.resistive, np.float32)
+        self.ctx.check(L.g3m3_model_set_inner(
+            h, addr(rst),
+            addr(li["ijsrf"]), addr(li["numsrf"]), addr(li["parm_srf"]), li["ijsrf"].shape[0],
+            addr(li["ijmid"]), addr(li["nummid"]), addr(li["parm_mid"]), li["ijmid"].shape[0],
+            addr(li["ijzero"]), addr(li["numzero"]), addr(li["parm_zero"]), li["ijzero"].shape[0]))
+        self.ctx.synchronize()
+
+    def init_steps(self):
+        self.ctx.check(self.L.g3m3_model_init_steps(self.h))
+
+    def run(self, nsteps: int, graph: bool = False):
+        self.ctx.check(self.L.g3m3_model_run(self.h, nsteps, 1 if graph else 0))
+
+    def divb_all(self):
+        rc = self.L.g3m3_model_divb_all(self.h)
+        if rc not in (0, 3):
+            self.ctx.check(rc)
+        return rc
+
+    def state(self, out=None):
+        p = self.p
+        if out is None:
+            out = np.empty((NFIELDS, p.n_grids, p.nz, p.ny, p.nx), np.float32)
+        self.ctx.check(self.L.g3m3_model_get_state(self.h, addr(out)))
+        return out
+
+    def set_state(self, arr):
+        self.ctx.check(self.L.g3m3_model_set_state(self.h, addr(arr)))
+
+    def field(self, which: int, q: int):
+        p = self.p
+        out = np.empty((p.n_grids, p.nz, p.ny, p.nx), np.float32)
+        self.ctx.check(self.L.g3m3_model_get_field(self.h, which, q, addr(out)))
+        return out
+
+    def times(self):
+        t = ctypes.c_double()
+        tsn = (ctypes.c_double * self.p.n_grids)()
+        cu = ctypes.c_int64()
+        self.ctx.check(self.L.g3m3_model_times(self.h, ctypes.byref(t), tsn, ctypes.byref(cu)))
+        return t.value, np.array(tsn[:]), cu.value
+
+    def stats(self):
+        k = ctypes.c_int64()
+        g = ctypes.c_int64()
+        self.ctx.check(self.L.g3m3_model_stats(self.h, ctypes.byref(k), ctypes.byref(g)))
+        return k.value, g.value
+
+    @property
+    def stream(self):
+        return self.L.g3m3_model_stream(self.h)
+
+    def close(self):
+        if self.h:
+            self.L.g3m3_model_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

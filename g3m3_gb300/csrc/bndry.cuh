@@ -1,0 +1,64 @@
+// bndry.cuh -- argument blocks of the boundary and nested-grid kernels.
+#pragma once
+
+#include "kargs.cuh"
+
+namespace g3m3 {
+
+struct OuterArgs {          // bndry_outer on the outermost box
+  float* f[G3M3_NFIELDS];
+  const float* b0[3];
+  Dims d;
+  float rmassq, rmassh, rmasso;
+  float srho, rho_frac, o_conc, spress, spx, spy, spz;
+  float sbx_wind, sby_wind, sbz_wind, ti_te;
+};
+
+struct InnerArgs {          // bndry_inner on box mbndry
+  float* f[G3M3_NFIELDS];
+  const int* ij[3];         // srf, mid, zero: (mbndry,3,m) column-major
+  const float* parm[3];     // (mbndry,7,m)
+  int num[3];
+  int mbndry, box;
+  Dims d;
+  float xmin, ymin, dx, dy, re_equiv, v_rot;
+};
+
+struct FlanksArgs {         // fine box shell from the time-interpolated coarse box
+  float* target[G3M3_NFIELDS];
+  const float* curc[G3M3_NFIELDS];
+  const float* oldc[G3M3_NFIELDS];
+  int nf;
+  Dims d;
+  ScalarRef t1;             // (t_new(mb)-t)/(t_new(mb)-t_old(mb)) rounded to FP32
+  float sxmin, symin, szmin, sx, sy, sz;        // fine box
+  float bxmin, bymin, bzmin, delx, dely, delz;  // coarse box
+};
+
+struct CorerArgs {          // coarse cells under the fine box from the fine box
+  float* coarse[G3M3_NFIELDS];
+  const float* fine[G3M3_NFIELDS];
+  int nf;
+  Dims d;
+  int nskip, nbx1, nby1, nbz1;
+  int ni, nj, nk;
+};
+
+struct SyncedArgs {         // flanks_synced
+  float* fine[G3M3_NFIELDS];
+  const float* coarse[G3M3_NFIELDS];
+  int nf;
+  Dims d;
+  float sxmin, symin, szmin, sx, sy, sz;
+  float bxmin, bymin, bzmin, delx, dely, delz;
+  int kb_top, kb_bot, jb_top, jb_bot, ib_top, ib_bot;
+};
+
+long shell_count(const Dims& d, int D);
+void launch_bndry_outer(const OuterArgs& a, cudaStream_t s);
+void launch_bndry_inner(const InnerArgs& a, cudaStream_t s);
+void launch_flanks(const FlanksArgs& a, cudaStream_t s);
+void launch_corer(const CorerArgs& a, cudaStream_t s);
+void launch_flanks_synced(const SyncedArgs& a, cudaStream_t s);
+
+}  // namespace g3m3

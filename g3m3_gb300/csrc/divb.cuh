@@ -1,0 +1,30 @@
+// divb.cuh -- state and arguments of the div B conjugate-gradient solver.
+#pragma once
+
+#include "kargs.cuh"
+
+namespace g3m3 {
+
+enum CgStatus : int { CG_RUNNING = 0, CG_CONVERGED = 1, CG_RESTART = 2, CG_MAXIT = 3, CG_GAVE_UP = 4 };
+
+struct CgState {          // lives in device memory
+  double anum, aden, r2, rsq, bsq, gg, dgg, errlim2, r2_last;
+  float gam, pad;
+  int status, iters, maxit, redos;
+};
+
+struct DivbArgs {
+  float *bx, *by, *bz;    // box slices, updated in place
+  float *rhs, *x, *xs, *g, *h, *xi, *xj;   // scratch vectors of one box
+  CgState* st;
+  Dims d;
+  float rx, ry, rz;
+};
+
+void divb_launch_init(const DivbArgs& a, cudaStream_t s);
+void divb_launch_restart(const DivbArgs& a, cudaStream_t s);
+void divb_launch_restore(const DivbArgs& a, cudaStream_t s);
+void divb_launch_iterations(const DivbArgs& a, int n, cudaStream_t s);
+void divb_launch_apply(const DivbArgs& a, cudaStream_t s);
+
+}  // namespace g3m3

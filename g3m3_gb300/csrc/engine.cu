@@ -1,0 +1,859 @@
+// engine.cu -- the multi-box step engine (g3m3_model_*): the reference's
+// main time loop (3d_main.f90:1925-3095) on device-resident state.
+//
+// Differences in mechanism (not in results) from the reference loop:
+//  * store_array (old <- cur, 34 copies per box-step, :2193-2229) is a
+//    rotation of the cur/old buffer roles.  Until the corrector writes cur,
+//    every read of cur is served from old (which then holds the same
+//    values), and the corrector pushes write the boundary cells of cur from
+//    old, so cur ends the push with the bits the reference has.
+//  * set_rho + set_speed_agrd run as one fused pass (k_guards.cu).
+//  * bs/btot are produced by the calcur kernel; BandE is one launch.
+//  * the time-dependent scalars of a main step (dt/2, dt, flank time
+//    weights) live in a small device table, so that one captured CUDA graph
+//    replays every main step with the same schedule shape.
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "ctx.cuh"
+
+namespace g3m3 {
+int run_divb(g3m3_ctx* c, float* bx, float* by, float* bz, const Dims& d, float rx, float errlim, CgState* st,
+             CgState* host_st, float* vec, cudaStream_t s, int* iters_out);
+void fill_flanks_geometry(FlanksArgs& a, int nx, int ny, int nz, int box, const float* gxmin, const float* gxmax,
+                          const float* gymin, const float* gymax, const float* gzmin, const float* gzmax);
+void fill_corer_geometry(CorerArgs& a, int nx, int ny, int nz, int box, const float* gxmin, const float* gxmax,
+                         const float* gymin, const float* gymax, const float* gzmin, const float* gzmax);
+void fill_synced_geometry(SyncedArgs& a, int nx, int ny, int nz, int box, const float* gxmin, const float* gxmax,
+                          const float* gymin, const float* gymax, const float* gzmin, const float* gzmax);
+void launch_bande_interior(const BandEArgs& a, cudaStream_t s);
+}  // namespace g3m3
+
+using namespace g3m3;
+
+struct g3m3_model {
+  g3m3_ctx* ctx = nullptr;
+  g3m3_params p{};
+  Dims d{};
+  size_t n3 = 0, n4 = 0;
+  float* mem = nullptr;              // one allocation for every array below
+  float* buf[3][G3M3_NFIELDS] = {};  // three full (nx,ny,nz,n_grids) copies per field
+  int role_cur[G3M3_MAX_GRIDS] = {}, role_old[G3M3_MAX_GRIDS] = {};
+  float* b0[3] = {};
+  float* resistive = nullptr;
+  float* rst_e = nullptr;            // BandE's resistive coefficient per cell (0: none)
+  bool lists_unique = true;
+  int* ij[3] = {};
+  float* parm[3] = {};
+  int num[3][G3M3_MAX_GRIDS] = {};
+  int mlen[3] = {};
+  bool inner_set = false;
+  float *efld[3], *curr[3], *bs[3], *btot, *ev[3], *tv[3], *vt[3];
+  float* glist = nullptr;
+  size_t gcap = 0;
+  unsigned* words = nullptr;         // [0] list count, [1..5] maxima scratch, [8+5b..] per-box maxima
+  unsigned* host_words = nullptr;
+  CgState* cg = nullptr;
+  CgState* host_cg = nullptr;
+  float* cgvec = nullptr;
+  float* d_scal = nullptr;
+  float* h_scal = nullptr;
+  int nscal = 0, scal_cap = 0;
+  double t = 0.0;
+  double t_old[G3M3_MAX_GRIDS] = {}, t_new[G3M3_MAX_GRIDS] = {};
+  double t_step[G3M3_MAX_GRIDS] = {}, t_stepnew[G3M3_MAX_GRIDS] = {};
+  int64_t cell_updates = 0;
+  int nsteps_done = 0;
+  float iso_flag = 1.0f;
+  int64_t kernels = 0, graph_launches = 0;
+  std::map<std::string, cudaGraphExec_t> graphs;
+  std::map<std::string, int64_t> kernel_nodes;
+  int64_t launches_in_step = 0;
+};
+
+namespace {
+
+inline float* F(g3m3_model* m, int role, int f, int box) { return m->buf[role][f] + (size_t)(box - 1) * m->n3; }
+inline float* C(g3m3_model* m, int f, int b) { return F(m, m->role_cur[b - 1], f, b); }
+inline float* O(g3m3_model* m, int f, int b) { return F(m, m->role_old[b - 1], f, b); }
+inline float* W(g3m3_model* m, int f, int b) { return F(m, 2, f, b); }
+
+using Getter = float* (*)(g3m3_model*, int, int);
+
+int scal_slot(g3m3_model* m, float v) {
+  if (m->nscal >= m->scal_cap) return -1;
+  m->h_scal[m->nscal] = v;
+  return m->nscal++;
+}
+
+ScalarRef sref(g3m3_model* m, int slot) { return ScalarRef{m->h_scal[slot], m->d_scal + slot}; }
+
+cudaStream_t S(g3m3_model* m) { return m->ctx->stream; }
+
+void fields_stage(g3m3_model* m, Getter src, int b) {
+  const float rx = m->p.xspac[b - 1];
+  CurrentArgs ca{};
+  for (int q = 0; q < 3; q++) {
+    ca.b[q] = src(m, G3M3_F_BX + q, b);
+    ca.b0[q] = m->b0[q] + (size_t)(b - 1) * m->n3;
+    ca.cur[q] = m->curr[q];
+    ca.bs[q] = m->bs[q];
+  }
+  ca.btot = m->btot;
+  ca.d = m->d; ca.rx = rx; ca.ry = rx; ca.rz = rx; ca.smallbit = m->p.smallbit;
+  launch_current(ca, S(m));
+  EvelArgs ea{};
+  for (int s = 0; s < 3; s++) {
+    for (int q = 0; q < 3; q++) ea.p[s][q] = src(m, 10 * s + 1 + q, b);
+    ea.rho[s] = src(m, 10 * s, b);
+  }
+  for (int q = 0; q < 3; q++) { ea.cur[q] = m->curr[q]; ea.ev[q] = m->ev[q]; ea.tv[q] = m->tv[q]; }
+  ea.d = m->d;
+  ea.rmass[0] = m->p.rmassq; ea.rmass[1] = m->p.rmassh; ea.rmass[2] = m->p.rmasso;
+  ea.reynolds = m->p.reynolds;
+  launch_evel(ea, S(m));
+  BandEArgs ba{};
+  for (int q = 0; q < 3; q++) {
+    ba.efld[q] = m->efld[q]; ba.bs[q] = m->bs[q]; ba.cur[q] = m->curr[q]; ba.ev[q] = m->ev[q];
+    ba.rho[q] = src(m, 10 * q, b);
+  }
+  ba.epres = src(m, G3M3_F_EPRES, b);
+  const bool resist = b <= m->p.mbndry && m->p.resist < 5000.0f && m->inner_set;
+  ba.rst_e = (resist && m->lists_unique) ? m->rst_e + (size_t)(b - 1) * m->n3 : nullptr;
+  ba.d = m->d;
+  ba.rmass[0] = m->p.rmassq; ba.rmass[1] = m->p.rmassh; ba.rmass[2] = m->p.rmasso;
+  ba.reynolds = m->p.reynolds; ba.rx = rx; ba.ry = rx; ba.rz = rx;
+  if (resist && !m->lists_unique) {
+    // lists with repeated cells: keep the reference's sequential scatter
+    launch_bande_interior(ba, S(m));
+    BandEListArgs l{};
+    for (int q = 0; q < 3; q++) { l.efld[q] = ba.efld[q]; l.cur[q] = ba.cur[q]; l.rho[q] = ba.rho[q]; l.rmass[q] = ba.rmass[q]; }
+    l.rst = m->resistive + (size_t)(b - 1) * m->n3;
+    l.mbndry = m->p.mbndry; l.box = b; l.d = m->d;
+    for (int q = 1; q < 3; q++) {
+      l.ij = m->ij[q];
+      l.count = m->num[q][b - 1];
+      launch_bande_list(l, S(m));
+    }
+    launch_bande_faces(ba.efld, m->d, S(m));
+    m->launches_in_step += 3;
+  } else {
+    launch_bande(ba, S(m));
+  }
+  m->launches_in_step += 3;
+}
+
+void push_stage(g3m3_model* m, Getter out, Getter src, int b, int slot_dt, bool out_is_cur) {
+  const float rx = m->p.xspac[b - 1];
+  PushFieldArgs pa{};
+  pa.wrkepres = W(m, G3M3_F_EPRES, b);
+  pa.oldepres = O(m, G3M3_F_EPRES, b);
+  pa.epres = C(m, G3M3_F_EPRES, b);
+  for (int q = 0; q < 3; q++) {
+    pa.ev[q] = m->ev[q];
+    pa.b[q] = out(m, G3M3_F_BX + q, b);
+    pa.oldb[q] = O(m, G3M3_F_BX + q, b);
+    pa.efld[q] = m->efld[q];
+  }
+  pa.d = m->d; pa.rx = rx; pa.ry = rx; pa.rz = rx; pa.gamma = m->p.gamma; pa.gamma1 = m->p.gamma1;
+  pa.delt = sref(m, slot_dt);
+  pa.do_elec = 1; pa.do_bfld = 1;
+  // cur's boundary must be the start-of-step state (see the file comment);
+  // epres always goes to cur, B goes to out
+  pa.boundary_from_old = 1;
+  if (!out_is_cur) {
+    // predictor: only epres lands in cur; B goes to wrk, whose boundary the
+    // reference leaves alone -- run the two pushes separately
+    PushFieldArgs e = pa;
+    e.do_bfld = 0;
+    launch_push_field(e, S(m));
+    PushFieldArgs bb = pa;
+    bb.do_elec = 0;
+    bb.boundary_from_old = 0;
+    launch_push_field(bb, S(m));
+    m->launches_in_step += 2;
+  } else {
+    launch_push_field(pa, S(m));
+    m->launches_in_step += 1;
+  }
+  const float masses[3] = {m->p.rmassq, m->p.rmassh, m->p.rmasso};
+  for (int s = 0; s < 3; s++) {
+    PushIonArgs a{};
+    for (int f = 0; f < 10; f++) {
+      a.out[f] = out(m, 10 * s + f, b);
+      a.old[f] = O(m, 10 * s + f, b);
+      a.src[f] = src(m, 10 * s + f, b);
+    }
+    for (int q = 0; q < 3; q++) { a.bs[q] = m->bs[q]; a.efld[q] = m->efld[q]; a.tv[q] = m->tv[q]; }
+    a.btot = m->btot;
+    a.d = m->d;
+    a.g.xmin = m->p.grd_xmin[b - 1]; a.g.ymin = m->p.grd_ymin[b - 1]; a.g.zmin = m->p.grd_zmin[b - 1];
+    a.g.dx = (m->p.grd_xmax[b - 1] - m->p.grd_xmin[b - 1]) / (float)(m->d.nx - 1);
+    a.g.dy = (m->p.grd_ymax[b - 1] - m->p.grd_ymin[b - 1]) / (float)(m->d.ny - 1);
+    a.g.dz = (m->p.grd_zmax[b - 1] - m->p.grd_zmin[b - 1]) / (float)(m->d.nz - 1);
+    a.rmass = masses[s]; a.grav = m->p.grav; a.re_equiv = m->p.re_equiv; a.reynolds = m->p.reynolds;
+    a.delt = sref(m, slot_dt);
+    a.boundary_from_old = out_is_cur ? 1 : 0;
+    launch_push_ion(a, S(m));
+    m->launches_in_step += 1;
+  }
+}
+
+void inner_stage(g3m3_model* m, Getter target) {
+  const g3m3_params& p = m->p;
+  InnerArgs a{};
+  const int mb = p.mbndry;   // bndry_inner always works on box mbndry
+  for (int q = 0; q < G3M3_NFIELDS; q++) a.f[q] = target(m, q, mb);
+  for (int l = 0; l < 3; l++) {
+    a.ij[l] = m->ij[l];
+    a.parm[l] = m->parm[l];
+    a.num[l] = m->num[l][mb - 1];
+  }
+  a.mbndry = mb; a.box = mb; a.d = m->d;
+  a.dx = (p.grd_xmax[mb - 1] - p.grd_xmin[mb - 1]) / ((float)m->d.nx - 1.0f);
+  a.dy = (p.grd_ymax[mb - 1] - p.grd_ymin[mb - 1]) / ((float)m->d.ny - 1.0f);
+  a.xmin = p.grd_xmin[mb - 1]; a.ymin = p.grd_ymin[mb - 1];
+  a.re_equiv = p.re_equiv; a.v_rot = p.v_rot;
+  launch_bndry_inner(a, S(m));
+  m->launches_in_step += 1;
+}
+
+void boundary_stage(g3m3_model* m, Getter target, int b, int slot_t1, Getter inner_target = nullptr) {
+  const g3m3_params& p = m->p;
+  const int ng = p.n_grids;
+  if (b == ng) {
+    OuterArgs a{};
+    for (int q = 0; q < G3M3_NFIELDS; q++) a.f[q] = target(m, q, b);
+    for (int q = 0; q < 3; q++) a.b0[q] = m->b0[q] + (size_t)(b - 1) * m->n3;
+    a.d = m->d;
+    a.rmassq = p.rmassq; a.rmassh = p.rmassh; a.rmasso = p.rmasso;
+    a.srho = p.srho; a.rho_frac = p.rho_frac; a.o_conc = p.o_conc; a.spress = p.spress;
+    a.spx = p.spx; a.spy = p.spy; a.spz = p.spz;
+    a.sbx_wind = p.sbx_wind; a.sby_wind = p.sby_wind; a.sbz_wind = p.sbz_wind; a.ti_te = p.ti_te;
+    launch_bndry_outer(a, S(m));
+  } else {
+    FlanksArgs a{};
+    for (int q = 0; q < G3M3_NFIELDS; q++) {
+      a.target[q] = target(m, q, b);
+      a.curc[q] = C(m, q, b + 1);
+      a.oldc[q] = O(m, q, b + 1);
+    }
+    a.nf = G3M3_NFIELDS;
+    fill_flanks_geometry(a, m->d.nx, m->d.ny, m->d.nz, b, p.grd_xmin, p.grd_xmax, p.grd_ymin, p.grd_ymax,
+                         p.grd_zmin, p.grd_zmax);
+    a.t1 = sref(m, slot_t1);
+    launch_flanks(a, S(m));
+  }
+  m->launches_in_step += 1;
+  if (b <= p.mbndry && m->inner_set) inner_stage(m, inner_target ? inner_target : target);
+}
+
+// set_rho and set_speed_agrd; maxima go to the box's slot when `record`
+int guard_stage(g3m3_model* m, Getter target, int b, bool speed, bool record) {
+  const g3m3_params& p = m->p;
+  GuardArgs a{};
+  for (int q = 0; q < G3M3_NFIELDS; q++) a.f[q] = target(m, q, b);
+  for (int q = 0; q < 3; q++) a.b0[q] = m->b0[q] + (size_t)(b - 1) * m->n3;
+  a.btot = m->btot;
+  a.d = m->d;
+  a.smallbit = p.smallbit; a.aniso_limit = p.aniso_limit; a.vlim = p.vlim_factor * (float)b;
+  a.svlim[0] = p.qvlim; a.svlim[1] = p.hvlim; a.svlim[2] = p.ovlim;
+  a.sclim[0] = p.qclim; a.sclim[1] = p.hclim; a.sclim[2] = p.oclim;
+  a.cslim = p.cslim; a.iso_flag = m->iso_flag; a.isotropic = p.isotropic != 0;
+  a.do_set_rho = 1; a.do_speed = speed ? 1 : 0;
+  a.list = m->glist; a.list_cap = (unsigned)m->gcap; a.list_count = m->words;
+  a.maxbits = record ? m->words + 8 + 5 * (b - 1) : m->words + 1;
+  const size_t zero_bytes = 6 * sizeof(unsigned);
+  cudaError_t e = cudaMemsetAsync(m->words, 0, zero_bytes, S(m));
+  if (e != cudaSuccess) return cuda_check(m->ctx, e, "memset guard words");
+  if (record) {
+    e = cudaMemsetAsync(m->words + 8 + 5 * (b - 1), 0, 5 * sizeof(unsigned), S(m));
+    if (e != cudaSuccess) return cuda_check(m->ctx, e, "memset box maxima");
+  }
+  launch_guards(a, S(m));
+  m->launches_in_step += 1;
+  if (speed) {
+    ScatterArgs sa{};
+    for (int q = 0; q < G3M3_NFIELDS; q++) sa.f[q] = a.f[q];
+    sa.list = m->glist; sa.list_count = m->words; sa.list_cap = (unsigned)m->gcap;
+    launch_guard_scatter(sa, S(m));
+    m->launches_in_step += 1;
+  }
+  return G3M3_OK;
+}
+
+void corer_stage(g3m3_model* m, int b) {
+  const g3m3_params& p = m->p;
+  CorerArgs a{};
+  for (int q = 0; q < G3M3_NFIELDS; q++) {
+    a.fine[q] = C(m, q, b);
+    a.coarse[q] = C(m, q, b + 1);
+  }
+  a.nf = G3M3_NFIELDS;
+  fill_corer_geometry(a, m->d.nx, m->d.ny, m->d.nz, b, p.grd_xmin, p.grd_xmax, p.grd_ymin, p.grd_ymax, p.grd_zmin,
+                      p.grd_zmax);
+  launch_corer(a, S(m));
+  m->launches_in_step += 1;
+}
+
+float flank_t1(g3m3_model* m, int b, double t_grid) {
+  const int mb = b + 1;
+  return (float)((m->t_new[mb - 1] - t_grid) / (m->t_new[mb - 1] - m->t_old[mb - 1]));
+}
+
+// One entry of a main step's plan.
+struct Action {
+  enum Kind { BOX_STEP, CORE_SYNC, FINAL_SYNC } kind;
+  int box;
+  int s_half, s_full, s_t1p, s_t1c;   // scalar-table slots
+};
+
+// Host-only: the reference's schedule for one main step (3d_main.f90:
+// 1929-1968, 2142-2165, 3044-3095).  Advances the host time bookkeeping,
+// fills the scalar table and returns the actions in launch order.
+int plan_main_step(g3m3_model* m, std::vector<Action>& acts) {
+  const g3m3_params& p = m->p;
+  const int ng = p.n_grids;
+  acts.clear();
+  m->nscal = 0;
+  double smallest_step = 0.0;
+  int m_smallest = ng;
+  for (int box = ng; box >= 1; box--) {
+    m->t_step[box - 1] = m->t_stepnew[box - 1];
+    m->t_old[box - 1] = 0.0;
+    m->t_new[box - 1] = 0.0;
+    if (box == ng) {
+      smallest_step = m->t_step[box - 1];
+      m_smallest = box;
+    } else {
+      if (m->t_step[box - 1] > m->t_step[box]) m->t_step[box - 1] = m->t_step[box];
+      if (smallest_step > m->t_step[box - 1]) {
+        smallest_step = m->t_step[box - 1];
+        m_smallest = box;
+      }
+    }
+  }
+  for (int box = 1; box <= ng; box++) {
+    if (box <= m_smallest) {
+      m->t_step[box - 1] = smallest_step;
+    } else {
+      const float astep = (float)(m->t_step[box - 1] / m->t_step[box - 2] + 0.50);
+      int nsteps = (int)astep;
+      if (nsteps > 2) nsteps = 2;
+      if (nsteps < 1) nsteps = 1;
+      m->t_step[box - 1] = m->t_step[box - 2] * nsteps;
+    }
+  }
+  const int m_step = (int)(m->t_step[ng - 1] / m->t_step[m_smallest - 1]);
+  const float delt_main = (float)m->t_step[ng - 1];
+  if (!(delt_main >= p.t_step_min))
+    return set_err(m->ctx, G3M3_ERR_STATE, "main time step %g below t_step_min", (double)delt_main);
+  m->t = m->t + (double)delt_main;
+  for (int ms = 1; ms <= m_step; ms++) {
+    for (int b = ng; b >= 1; b--) {
+      bool yes = b == 1;
+      if (!yes && m->t_old[b - 1] == m->t_new[b - 1] && m->t_new[b - 1] < m->t_step[ng - 1] &&
+          std::fabs(m->t_new[b - 1] - m->t_new[0]) <= (double)0.005f * m->t_step[0])
+        yes = true;
+      if (!yes) continue;
+      Action a{Action::BOX_STEP, b, -1, -1, -1, -1};
+      m->t_old[b - 1] = m->t_new[b - 1];
+      m->t_new[b - 1] = m->t_old[b - 1] + m->t_step[b - 1];
+      const float delt = (float)m->t_step[b - 1];
+      const float delt2 = delt / 2.0f;
+      a.s_half = scal_slot(m, 0.5f * delt);
+      a.s_full = scal_slot(m, delt);
+      if (b < ng) {
+        double tg = m->t_old[b - 1] + (double)delt2;
+        if (tg > m->t_new[b]) tg = m->t_new[b];
+        if (tg < m->t_old[b]) tg = m->t_old[b];
+        a.s_t1p = scal_slot(m, flank_t1(m, b, tg));
+        tg = m->t_old[b - 1] + (double)delt;
+        if (tg > m->t_new[b]) tg = m->t_new[b];
+        if (tg < m->t_old[b]) tg = m->t_old[b];
+        a.s_t1c = scal_slot(m, flank_t1(m, b, tg));
+        if (a.s_t1p < 0 || a.s_t1c < 0) return set_err(m->ctx, G3M3_ERR_STATE, "scalar table full");
+      }
+      if (a.s_half < 0 || a.s_full < 0) return set_err(m->ctx, G3M3_ERR_STATE, "scalar table full");
+      acts.push_back(a);
+      m->cell_updates += (int64_t)m->n3;
+      if (b < ng && std::fabs(m->t_new[b - 1] - m->t_new[b]) <= (double)0.005f * m->t_step[b - 1]) {
+        acts.push_back(Action{Action::CORE_SYNC, b, -1, -1, -1, -1});
+        m->t_old[b] = m->t_new[b];
+      }
+    }
+  }
+  m->t_old[0] = m->t_new[0];
+  for (int b = 1; b <= ng - 1; b++) {
+    acts.push_back(Action{Action::FINAL_SYNC, b, -1, -1, -1, -1});
+    if (b > 1) {  // the reference reads t_old(0) for box 1 (3d_main.f90:3093)
+      m->t_old[b - 1] = m->t_old[b - 2];
+      m->t_new[b - 1] = m->t_new[b - 2];
+    }
+  }
+  return G3M3_OK;
+}
+
+std::string plan_key(g3m3_model* m, const std::vector<Action>& acts) {
+  std::string k;
+  for (int b = 0; b < m->p.n_grids; b++) k += char('0' + m->role_cur[b]);
+  k += ':';
+  for (const Action& a : acts) {
+    k += a.kind == Action::BOX_STEP ? 's' : (a.kind == Action::CORE_SYNC ? 'c' : 'f');
+    k += std::to_string(a.box);
+  }
+  return k;
+}
+
+void apply_role_swaps(g3m3_model* m, const std::vector<Action>& acts) {
+  for (const Action& a : acts)
+    if (a.kind == Action::BOX_STEP) std::swap(m->role_cur[a.box - 1], m->role_old[a.box - 1]);
+}
+
+// Launch the kernels of one box-step (predictor, corrector, Lapidus, flux
+// correction, each followed by boundaries and guards; 3d_main.f90:2170-3039).
+int enqueue_box_step(g3m3_model* m, const Action& act) {
+  const g3m3_params& p = m->p;
+  const int ng = p.n_grids, b = act.box;
+  std::swap(m->role_cur[b - 1], m->role_old[b - 1]);   // store_array
+  int st;
+  // predictor (reads of cur are served from old, which holds the same data)
+  fields_stage(m, O, b);
+  push_stage(m, W, O, b, act.s_half, false);
+  boundary_stage(m, W, b, act.s_t1p);
+  if ((st = guard_stage(m, W, b, true, false))) return st;
+  // corrector
+  fields_stage(m, W, b);
+  push_stage(m, C, W, b, act.s_full, true);
+  if (b == ng) {
+    boundary_stage(m, C, b, -1);
+  } else {
+    // the reference applies the corrector's flanks to the wrk arrays
+    // (3d_main.f90:2599-2637) and bndry_inner to cur (:2640-2658)
+    boundary_stage(m, W, b, act.s_t1c, C);
+  }
+  if ((st = guard_stage(m, C, b, true, false))) return st;
+  // Lapidus smoothing (3d_main.f90:2690-2772)
+  for (int s = 0; s < 3; s++) {
+    LapArgs la{};
+    for (int f = 0; f < 10; f++) {
+      la.in[f] = C(m, 10 * s + f, b);
+      la.out[f] = W(m, 10 * s + f, b);
+      la.chi[f] = f == 0 ? p.chirho : p.chipxyz;
+    }
+    la.nf = 10;
+    for (int q = 0; q < 3; q++) la.vp[q] = C(m, 10 * s + 1 + q, b);
+    la.vrho = C(m, 10 * s, b);
+    la.vfloor = p.smallbit;
+    la.d = m->d;
+    la.delt = sref(m, act.s_full);
+    launch_lap(la, S(m));
+  }
+  VtotArgs va{};
+  for (int s = 0; s < 3; s++) {
+    for (int q = 0; q < 3; q++) va.p[s][q] = C(m, 10 * s + 1 + q, b);
+    va.rho[s] = C(m, 10 * s, b);
+  }
+  for (int q = 0; q < 3; q++) va.v[q] = m->vt[q];
+  va.d = m->d;
+  launch_vtot(va, S(m));
+  LapArgs lb{};
+  lb.in[0] = C(m, G3M3_F_EPRES, b); lb.out[0] = W(m, G3M3_F_EPRES, b); lb.chi[0] = p.chipxyz;
+  for (int q = 0; q < 3; q++) {
+    lb.in[1 + q] = C(m, G3M3_F_BX + q, b);
+    lb.out[1 + q] = W(m, G3M3_F_BX + q, b);
+    lb.chi[1 + q] = p.chierg;
+    lb.v[q] = m->vt[q];
+  }
+  lb.nf = 4; lb.d = m->d; lb.delt = sref(m, act.s_full);
+  launch_lap(lb, S(m));
+  m->launches_in_step += 5;
+  boundary_stage(m, W, b, act.s_t1c);
+  if ((st = guard_stage(m, W, b, true, false))) return st;
+  // flux correction (3d_main.f90:2896-3036)
+  FcsArgs fa{};
+  for (int q = 0; q < G3M3_NFIELDS; q++) {
+    fa.px[q] = C(m, q, b);
+    fa.old[q] = O(m, q, b);
+    fa.wrk[q] = W(m, q, b);
+    fa.chi[q] = q >= G3M3_F_BX ? p.diferg : p.difrho;
+  }
+  fa.nf = G3M3_NFIELDS; fa.d = m->d;
+  launch_fcsmooth(fa, S(m));
+  m->launches_in_step += 1;
+  boundary_stage(m, C, b, act.s_t1c);
+  return guard_stage(m, C, b, true, true);
+}
+
+int enqueue_plan(g3m3_model* m, const std::vector<Action>& acts) {
+  for (const Action& a : acts) {
+    int st = G3M3_OK;
+    switch (a.kind) {
+      case Action::BOX_STEP: st = enqueue_box_step(m, a); break;
+      case Action::CORE_SYNC: corer_stage(m, a.box); break;
+      case Action::FINAL_SYNC:
+        corer_stage(m, a.box);
+        st = guard_stage(m, C, a.box, false, false);
+        break;
+    }
+    if (st) return st;
+  }
+  return G3M3_OK;
+}
+
+// t_stepnew(box) from the recorded maxima (3d_main.f90:3038-3039)
+void finish_steps(g3m3_model* m, int box_lo, int box_hi) {
+  for (int b = box_lo; b <= box_hi; b++) {
+    const unsigned* w = m->host_words + 8 + 5 * (b - 1);
+    float v[5];
+    for (int q = 0; q < 5; q++) std::memcpy(&v[q], &w[q], sizeof(float));
+    float fastest = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2] + v[3] * v[3] + v[4] * v[4]);
+    fastest = 0.0f > fastest ? 0.0f : fastest;
+    const float a = m->p.stepsz * m->p.xspac[b - 1] / fastest;
+    m->t_stepnew[b - 1] = (double)(a < m->p.t_step_max ? a : m->p.t_step_max);
+  }
+}
+
+int alloc_model(g3m3_model* m) {
+  const size_t n3 = m->n3, n4 = m->n4;
+  const int mb = m->p.mbndry;
+  size_t total = 3 * G3M3_NFIELDS * n4 + 3 * n4 + 2 * (size_t)mb * n3 + 19 * n3 + 7 * n3;
+  cudaError_t e = cudaMalloc(&m->mem, total * sizeof(float));
+  if (e != cudaSuccess) return cuda_check(m->ctx, e, "cudaMalloc(model)");
+  e = cudaMemsetAsync(m->mem, 0, total * sizeof(float), m->ctx->stream);
+  if (e != cudaSuccess) return cuda_check(m->ctx, e, "memset(model)");
+  float* q = m->mem;
+  for (int r = 0; r < 3; r++)
+    for (int f = 0; f < G3M3_NFIELDS; f++) { m->buf[r][f] = q; q += n4; }
+  for (int c = 0; c < 3; c++) { m->b0[c] = q; q += n4; }
+  m->resistive = q; q += (size_t)mb * n3;
+  m->rst_e = q; q += (size_t)mb * n3;
+  float** scr[19] = {&m->efld[0], &m->efld[1], &m->efld[2], &m->curr[0], &m->curr[1], &m->curr[2],
+                     &m->bs[0],   &m->bs[1],   &m->bs[2],   &m->btot,    &m->ev[0],   &m->ev[1],
+                     &m->ev[2],   &m->tv[0],   &m->tv[1],   &m->tv[2],   &m->vt[0],   &m->vt[1],
+                     &m->vt[2]};
+  for (int i = 0; i < 19; i++) { *scr[i] = q; q += n3; }
+  m->cgvec = q; q += 7 * n3;
+  m->gcap = 3 * n3;
+  e = cudaMalloc(&m->glist, m->gcap * 11 * sizeof(float));
+  if (e != cudaSuccess) return cuda_check(m->ctx, e, "cudaMalloc(limiter list)");
+  const size_t nwords = 8 + 5 * (size_t)G3M3_MAX_GRIDS;
+  if ((e = cudaMalloc(&m->words, nwords * sizeof(unsigned))) != cudaSuccess) return cuda_check(m->ctx, e, "words");
+  if ((e = cudaMemsetAsync(m->words, 0, nwords * sizeof(unsigned), m->ctx->stream)) != cudaSuccess)
+    return cuda_check(m->ctx, e, "words");
+  if ((e = cudaMallocHost(&m->host_words, nwords * sizeof(unsigned))) != cudaSuccess)
+    return cuda_check(m->ctx, e, "host words");
+  if ((e = cudaMalloc(&m->cg, sizeof(CgState))) != cudaSuccess) return cuda_check(m->ctx, e, "cg");
+  if ((e = cudaMallocHost(&m->host_cg, sizeof(CgState))) != cudaSuccess) return cuda_check(m->ctx, e, "cg");
+  m->scal_cap = 4096;
+  if ((e = cudaMalloc(&m->d_scal, m->scal_cap * sizeof(float))) != cudaSuccess) return cuda_check(m->ctx, e, "scal");
+  if ((e = cudaMallocHost(&m->h_scal, m->scal_cap * sizeof(float))) != cudaSuccess)
+    return cuda_check(m->ctx, e, "scal");
+  for (int b = 0; b < G3M3_MAX_GRIDS; b++) { m->role_cur[b] = 0; m->role_old[b] = 1; }
+  return G3M3_OK;
+}
+
+int copy_in(g3m3_model* m, float* dst, const float* src, size_t n) {
+  cudaError_t e = cudaMemcpyAsync(dst, src, n * sizeof(float), cudaMemcpyDefault, m->ctx->stream);
+  return e == cudaSuccess ? G3M3_OK : cuda_check(m->ctx, e, "cudaMemcpyAsync");
+}
+
+}  // namespace
+
+extern "C" {
+
+int g3m3_model_create(g3m3_ctx* ctx, const g3m3_params* p, g3m3_model** out) {
+  if (!ctx || !p || !out) return G3M3_ERR_ARG;
+  *out = nullptr;
+  if (p->nx < 5 || p->ny < 5 || p->nz < 5 || p->n_grids < 1 || p->n_grids > G3M3_MAX_GRIDS || p->mbndry < 1 ||
+      p->mbndry > p->n_grids)
+    return set_err(ctx, G3M3_ERR_ARG, "bad model dimensions");
+  g3m3_model* m = new g3m3_model();
+  m->ctx = ctx;
+  m->p = *p;
+  m->d = Dims{p->nx, p->ny, p->nz};
+  m->n3 = m->d.cells();
+  m->n4 = m->n3 * p->n_grids;
+  int st = alloc_model(m);
+  if (st) {
+    g3m3_model_destroy(m);
+    return st;
+  }
+  *out = m;
+  return G3M3_OK;
+}
+
+int g3m3_model_destroy(g3m3_model* m) {
+  if (!m) return G3M3_ERR_ARG;
+  cudaStreamSynchronize(m->ctx->stream);
+  for (auto& kv : m->graphs) cudaGraphExecDestroy(kv.second);
+  if (m->mem) cudaFree(m->mem);
+  if (m->glist) cudaFree(m->glist);
+  if (m->words) cudaFree(m->words);
+  if (m->host_words) cudaFreeHost(m->host_words);
+  if (m->cg) cudaFree(m->cg);
+  if (m->host_cg) cudaFreeHost(m->host_cg);
+  if (m->d_scal) cudaFree(m->d_scal);
+  if (m->h_scal) cudaFreeHost(m->h_scal);
+  for (int l = 0; l < 3; l++) {
+    if (m->ij[l]) cudaFree(m->ij[l]);
+    if (m->parm[l]) cudaFree(m->parm[l]);
+  }
+  delete m;
+  return G3M3_OK;
+}
+
+void* g3m3_model_stream(g3m3_model* m) { return m ? (void*)m->ctx->stream : nullptr; }
+
+int g3m3_model_set_field(g3m3_model* m, int which, int field, const float* data) {
+  if (!m || !data || field < 0 || field >= G3M3_NFIELDS || which < 0 || which > 2) return G3M3_ERR_ARG;
+  // `which` names the logical copy; every box shares the same role mapping
+  // only before the first step, so per-box roles are honoured here
+  for (int b = 1; b <= m->p.n_grids; b++) {
+    float* dst = which == 0 ? C(m, field, b) : (which == 1 ? O(m, field, b) : W(m, field, b));
+    int st = copy_in(m, dst, data + (size_t)(b - 1) * m->n3, m->n3);
+    if (st) return st;
+  }
+  return G3M3_OK;
+}
+
+int g3m3_model_get_field(g3m3_model* m, int which, int field, float* data) {
+  if (!m || !data || field < 0 || field >= G3M3_NFIELDS || which < 0 || which > 2) return G3M3_ERR_ARG;
+  for (int b = 1; b <= m->p.n_grids; b++) {
+    const float* src = which == 0 ? C(m, field, b) : (which == 1 ? O(m, field, b) : W(m, field, b));
+    cudaError_t e = cudaMemcpyAsync(data + (size_t)(b - 1) * m->n3, src, m->n3 * sizeof(float), cudaMemcpyDefault,
+                                    m->ctx->stream);
+    if (e != cudaSuccess) return cuda_check(m->ctx, e, "get_field");
+  }
+  cudaError_t e = cudaStreamSynchronize(m->ctx->stream);
+  return e == cudaSuccess ? G3M3_OK : cuda_check(m->ctx, e, "get_field sync");
+}
+
+int g3m3_model_set_state(g3m3_model* m, const float* data) {
+  if (!m || !data) return G3M3_ERR_ARG;
+  for (int f = 0; f < G3M3_NFIELDS; f++) {
+    int st = g3m3_model_set_field(m, 0, f, data + (size_t)f * m->n4);
+    if (st) return st;
+  }
+  return G3M3_OK;
+}
+
+int g3m3_model_get_state(g3m3_model* m, float* data) {
+  if (!m || !data) return G3M3_ERR_ARG;
+  for (int f = 0; f < G3M3_NFIELDS; f++)
+    for (int b = 1; b <= m->p.n_grids; b++) {
+      cudaError_t e = cudaMemcpyAsync(data + (size_t)f * m->n4 + (size_t)(b - 1) * m->n3, C(m, f, b),
+                                      m->n3 * sizeof(float), cudaMemcpyDefault, m->ctx->stream);
+      if (e != cudaSuccess) return cuda_check(m->ctx, e, "get_state");
+    }
+  cudaError_t e = cudaStreamSynchronize(m->ctx->stream);
+  return e == cudaSuccess ? G3M3_OK : cuda_check(m->ctx, e, "get_state sync");
+}
+
+int g3m3_model_set_b0(g3m3_model* m, const float* bx0, const float* by0, const float* bz0) {
+  if (!m || !bx0 || !by0 || !bz0) return G3M3_ERR_ARG;
+  const float* s[3] = {bx0, by0, bz0};
+  for (int q = 0; q < 3; q++) {
+    int st = copy_in(m, m->b0[q], s[q], m->n4);
+    if (st) return st;
+  }
+  return G3M3_OK;
+}
+
+int g3m3_model_set_inner(g3m3_model* m, const float* resistive, const int* ijsrf, const int* numsrf,
+                         const float* parm_srf, int msrf, const int* ijmid, const int* nummid, const float* parm_mid,
+                         int mmid, const int* ijzero, const int* numzero, const float* parm_zero, int mzero) {
+  if (!m || !resistive || !ijsrf || !numsrf || !parm_srf || !ijmid || !nummid || !parm_mid || !ijzero || !numzero ||
+      !parm_zero || msrf < 1 || mmid < 1 || mzero < 1)
+    return G3M3_ERR_ARG;
+  const int mb = m->p.mbndry;
+  const int* ij[3] = {ijsrf, ijmid, ijzero};
+  const int* num[3] = {numsrf, nummid, numzero};
+  const float* parm[3] = {parm_srf, parm_mid, parm_zero};
+  const int ml[3] = {msrf, mmid, mzero};
+  cudaError_t e;
+  for (int l = 0; l < 3; l++) {
+    for (int b = 0; b < mb; b++) {
+      if (num[l][b] < 0 || num[l][b] > ml[l]) return set_err(m->ctx, G3M3_ERR_ARG, "inner list count out of range");
+      m->num[l][b] = num[l][b];
+    }
+    m->mlen[l] = ml[l];
+    if (m->ij[l]) cudaFree(m->ij[l]);
+    if (m->parm[l]) cudaFree(m->parm[l]);
+    m->ij[l] = nullptr;
+    m->parm[l] = nullptr;
+    if ((e = cudaMalloc(&m->ij[l], (size_t)mb * 3 * ml[l] * sizeof(int))) != cudaSuccess)
+      return cuda_check(m->ctx, e, "lists");
+    if ((e = cudaMalloc(&m->parm[l], (size_t)mb * 7 * ml[l] * sizeof(float))) != cudaSuccess)
+      return cuda_check(m->ctx, e, "parms");
+    if ((e = cudaMemcpy(m->ij[l], ij[l], (size_t)mb * 3 * ml[l] * sizeof(int), cudaMemcpyDefault)) != cudaSuccess)
+      return cuda_check(m->ctx, e, "lists");
+    if ((e = cudaMemcpy(m->parm[l], parm[l], (size_t)mb * 7 * ml[l] * sizeof(float), cudaMemcpyDefault)) !=
+        cudaSuccess)
+      return cuda_check(m->ctx, e, "parms");
+  }
+  // BandE's per-cell resistive coefficient: rst at the ijmid and ijzero
+  // cells (sub_BandE.f90:191-219), 0 elsewhere
+  std::vector<float> rst((size_t)mb * m->n3), rste((size_t)mb * m->n3, 0.0f);
+  std::vector<unsigned char> seen((size_t)mb * m->n3, 0);
+  if ((e = cudaMemcpy(rst.data(), resistive, rst.size() * sizeof(float), cudaMemcpyDefault)) != cudaSuccess)
+    return cuda_check(m->ctx, e, "resistive");
+  m->lists_unique = true;
+  for (int b = 1; b <= mb; b++)
+    for (int l = 1; l < 3; l++)
+      for (int n = 0; n < m->num[l][b - 1]; n++) {
+        const int i = ij[l][(b - 1) + (size_t)mb * (0 + 3 * (size_t)n)];
+        const int j = ij[l][(b - 1) + (size_t)mb * (1 + 3 * (size_t)n)];
+        const int k = ij[l][(b - 1) + (size_t)mb * (2 + 3 * (size_t)n)];
+        if (i < 2 || j < 2 || k < 2 || i >= m->d.nx || j >= m->d.ny || k >= m->d.nz) {
+          m->lists_unique = false;   // a boundary cell: keep the reference's order
+          continue;
+        }
+        const size_t c = (size_t)(b - 1) * m->n3 + m->d.at(i, j, k);
+        if (seen[c] || rst[c] == 0.0f) m->lists_unique = false;
+        seen[c] = 1;
+        rste[c] = rst[c];
+      }
+  if ((e = cudaMemcpy(m->resistive, rst.data(), rst.size() * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess)
+    return cuda_check(m->ctx, e, "resistive");
+  if ((e = cudaMemcpy(m->rst_e, rste.data(), rste.size() * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess)
+    return cuda_check(m->ctx, e, "rst_e");
+  m->inner_set = true;
+  return G3M3_OK;
+}
+
+int g3m3_model_init_steps(g3m3_model* m) {
+  if (!m) return G3M3_ERR_ARG;
+  for (int b = m->p.n_grids; b >= 1; b--) {
+    m->t_old[b - 1] = 0.0;
+    m->t_new[b - 1] = 0.0;
+    int st = guard_stage(m, C, b, true, true);
+    if (st) return st;
+  }
+  cudaError_t e = cudaMemcpyAsync(m->host_words, m->words, (8 + 5 * (size_t)G3M3_MAX_GRIDS) * sizeof(unsigned),
+                                  cudaMemcpyDeviceToHost, m->ctx->stream);
+  if (e != cudaSuccess) return cuda_check(m->ctx, e, "init readback");
+  if ((e = cudaStreamSynchronize(m->ctx->stream)) != cudaSuccess) return cuda_check(m->ctx, e, "init sync");
+  finish_steps(m, 1, m->p.n_grids);
+  return G3M3_OK;
+}
+
+int g3m3_model_divb_all(g3m3_model* m) {
+  if (!m) return G3M3_ERR_ARG;
+  const g3m3_params& p = m->p;
+  const int ng = p.n_grids;
+  int worst = G3M3_OK;
+  for (int b = ng; b >= 1; b--)
+    for (int rep = 0; rep < 2; rep++) {
+      int it = 0;
+      int st = run_divb(m->ctx, C(m, G3M3_F_BX, b), C(m, G3M3_F_BY, b), C(m, G3M3_F_BZ, b), m->d, p.xspac[b - 1],
+                        p.divb_errlim, m->cg, m->host_cg, m->cgvec, m->ctx->stream, &it);
+      if (st == G3M3_ERR_NOCONV) worst = st;
+      else if (st) return st;
+    }
+  for (int b = ng - 1; b >= 1; b--) {
+    SyncedArgs a{};
+    for (int q = 0; q < 3; q++) {
+      a.fine[q] = C(m, G3M3_F_BX + q, b);
+      a.coarse[q] = C(m, G3M3_F_BX + q, b + 1);
+    }
+    a.nf = 3;
+    fill_synced_geometry(a, m->d.nx, m->d.ny, m->d.nz, b, p.grd_xmin, p.grd_xmax, p.grd_ymin, p.grd_ymax,
+                         p.grd_zmin, p.grd_zmax);
+    launch_flanks_synced(a, m->ctx->stream);
+  }
+  for (int b = 1; b <= ng - 1; b++) corer_stage(m, b);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_check(m->ctx, e, "divb_all");
+  return worst;
+}
+
+int g3m3_model_run(g3m3_model* m, int nsteps, int use_graph) {
+  if (!m || nsteps < 0) return G3M3_ERR_ARG;
+  m->kernels = 0;
+  m->graph_launches = 0;
+  const size_t nwords = 8 + 5 * (size_t)G3M3_MAX_GRIDS;
+  cudaStream_t s = m->ctx->stream;
+  std::vector<Action> acts;
+  for (int it = 0; it < nsteps; it++) {
+    const std::string roles = plan_key(m, {});
+    int rc = plan_main_step(m, acts);
+    if (rc) return rc;
+    std::string key = roles + plan_key(m, acts).substr(m->p.n_grids + 1);
+    cudaError_t e;
+    m->launches_in_step = 0;
+    if (use_graph) {
+      auto found = m->graphs.find(key);
+      if (found == m->graphs.end()) {
+        // capture: scalar upload from the pinned table, the step, and the
+        // read-back of the recorded maxima
+        int rcur[G3M3_MAX_GRIDS], rold[G3M3_MAX_GRIDS];
+        std::memcpy(rcur, m->role_cur, sizeof rcur);
+        std::memcpy(rold, m->role_old, sizeof rold);
+        cudaGraph_t g = nullptr;
+        if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+          return cuda_check(m->ctx, e, "begin capture");
+        cudaError_t e1 = cudaMemcpyAsync(m->d_scal, m->h_scal, m->scal_cap * sizeof(float), cudaMemcpyHostToDevice, s);
+        rc = enqueue_plan(m, acts);
+        cudaError_t e3 = cudaMemcpyAsync(m->host_words, m->words, nwords * sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+        cudaError_t e2 = cudaStreamEndCapture(s, &g);
+        std::memcpy(m->role_cur, rcur, sizeof rcur);   // capture did not run anything
+        std::memcpy(m->role_old, rold, sizeof rold);
+        if (rc || e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
+          if (g) cudaGraphDestroy(g);
+          if (rc) return rc;
+          return cuda_check(m->ctx, e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3), "graph capture");
+        }
+        cudaGraphExec_t ex = nullptr;
+        e = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_check(m->ctx, e, "graph instantiate");
+        found = m->graphs.emplace(key, ex).first;
+        m->kernel_nodes[key] = m->launches_in_step;
+      }
+      if ((e = cudaGraphLaunch(found->second, s)) != cudaSuccess) return cuda_check(m->ctx, e, "graph launch");
+      apply_role_swaps(m, acts);
+      m->graph_launches += 1;
+      m->kernels += m->kernel_nodes[key];
+    } else {
+      if ((e = cudaMemcpyAsync(m->d_scal, m->h_scal, (size_t)m->nscal * sizeof(float), cudaMemcpyHostToDevice, s)) !=
+          cudaSuccess)
+        return cuda_check(m->ctx, e, "scalar upload");
+      if ((rc = enqueue_plan(m, acts))) return rc;
+      if ((e = cudaMemcpyAsync(m->host_words, m->words, nwords * sizeof(unsigned), cudaMemcpyDeviceToHost, s)) !=
+          cudaSuccess)
+        return cuda_check(m->ctx, e, "readback");
+      m->kernels += m->launches_in_step;
+    }
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(m->ctx, e, "main step");
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(m->ctx, e, "main step");
+    finish_steps(m, 1, m->p.n_grids);
+    m->nsteps_done += 1;
+    if (m->p.divb_every > 0 && (m->nsteps_done % m->p.divb_every) == 0) {
+      const int st = g3m3_model_divb_all(m);
+      if (st && st != G3M3_ERR_NOCONV) return st;
+      if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(m->ctx, e, "divb");
+    }
+  }
+  return G3M3_OK;
+}
+
+int g3m3_model_times(g3m3_model* m, double* t, double* t_stepnew, int64_t* cell_updates) {
+  if (!m) return G3M3_ERR_ARG;
+  if (t) *t = m->t;
+  if (t_stepnew) std::memcpy(t_stepnew, m->t_stepnew, m->p.n_grids * sizeof(double));
+  if (cell_updates) *cell_updates = m->cell_updates;
+  return G3M3_OK;
+}
+
+int g3m3_model_stats(g3m3_model* m, int64_t* kernels, int64_t* graphs) {
+  if (!m) return G3M3_ERR_ARG;
+  if (kernels) *kernels = m->kernels;
+  if (graphs) *graphs = m->graph_launches;
+  return G3M3_OK;
+}
+
+}  // extern "C"

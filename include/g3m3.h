@@ -1,0 +1,329 @@
+/*
+ * g3m3.h -- C ABI of the GB300-native G3M^3 multifluid step
+ * (libg3m3_gpu.so, sm_103a).
+ *
+ * Two layers:
+ *
+ * 1. Drop-in routines.  One entry point per reference subroutine on the
+ *    time-step path, taking the reference's dummy arguments in the same
+ *    order (file:line of each below).  Arrays follow the Fortran layout
+ *    A(nx,ny,nz,n_grids) / A(nx,ny,nz), column-major FP32, and may be either
+ *    device pointers or host arrays.  A host array is mirrored on the device
+ *    the first time the library sees it (keyed by its base address) and
+ *    stays resident; results are written to the mirror.  Call
+ *    g3m3_sync_to_host() before host code reads an array the library wrote,
+ *    and g3m3_sync_to_device() after host code changed an array the library
+ *    has mirrored.  Scalars the Fortran only reads are passed by value;
+ *    scalars it returns are pointers.  Every routine returns a status
+ *    (G3M3_OK = 0); g3m3_last_error() describes the last failure.  The
+ *    reference prints and stops instead (3d_main.f90:1970-1974); a caller
+ *    keeps that behaviour by stopping on a nonzero status.
+ *
+ * 2. The step engine.  g3m3_model_* keeps a whole multi-box state on the
+ *    device and runs the reference's main loop (3d_main.f90:1925-3095: time
+ *    step schedule, sub-cycling, predictor, corrector, Lapidus smoothing,
+ *    flux correction, boundaries, nested-grid sync) with fused kernels,
+ *    buffer rotation instead of store_array copies, and optionally one CUDA
+ *    graph per main step.
+ *
+ * Threading: a context has one CUDA stream and must not be used from two
+ * host threads at once.  All calls are asynchronous on that stream unless
+ * they return a host value.
+ */
+#ifndef G3M3_H
+#define G3M3_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "g3m3_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define G3M3_OK 0
+#define G3M3_ERR_ARG 1       /* bad dimensions, box index or pointer      */
+#define G3M3_ERR_CUDA 2      /* a CUDA call failed                        */
+#define G3M3_ERR_NOCONV 3    /* div B solver stopped without converging   */
+#define G3M3_ERR_NONFINITE 4 /* a check found NaN or Inf                  */
+#define G3M3_ERR_ALLOC 5     /* device allocation failed                  */
+#define G3M3_ERR_STATE 6     /* call out of order                         */
+
+typedef struct g3m3_ctx g3m3_ctx;
+typedef struct g3m3_model g3m3_model;
+
+/* ---- context -------------------------------------------------------- */
+int g3m3_ctx_create(g3m3_ctx** out, int device);
+int g3m3_ctx_destroy(g3m3_ctx* ctx);
+const char* g3m3_last_error(g3m3_ctx* ctx);
+/* Copy the device mirror of a host array back to it / refresh the mirror
+ * from the host array.  Device pointers are accepted and ignored. */
+int g3m3_sync_to_host(g3m3_ctx* ctx, void* host_array);
+int g3m3_sync_to_device(g3m3_ctx* ctx, const void* host_array);
+/* Drop every mirror (their device memory is freed). */
+int g3m3_release_mirrors(g3m3_ctx* ctx);
+int g3m3_synchronize(g3m3_ctx* ctx);
+/* Library build description (kernel arch, flags). */
+const char* g3m3_version(void);
+
+/* ---- a1: push_ion -- sub_push_ion.f90:4-17 ---------------------------- */
+int g3m3_push_ion(g3m3_ctx* ctx,
+    float* qrho, float* qpresx, float* qpresy, float* qpresz,
+    float* qpx, float* qpy, float* qpz,
+    const float* oldqrho, const float* oldqpresx, const float* oldqpresy,
+    const float* oldqpresz, const float* oldqpx, const float* oldqpy,
+    const float* oldqpz,
+    const float* wrkqrho, const float* wrkqpresx, const float* wrkqpresy,
+    const float* wrkqpresz, const float* wrkqpx, const float* wrkqpy,
+    const float* wrkqpz,
+    float* qpresxy, float* qpresxz, float* qpresyz,
+    const float* oldqpresxy, const float* oldqpresxz, const float* oldqpresyz,
+    const float* wrkqpresxy, const float* wrkqpresxz, const float* wrkqpresyz,
+    const float* bsx, const float* bsy, const float* bsz, const float* btot,
+    const float* efldx, const float* efldy, const float* efldz, float rmassq,
+    float* qvx, float* qvy, float* qvz,
+    const float* tvx, const float* tvy, const float* tvz,
+    float gamma, float gamma1,
+    int nx, int ny, int nz, int n_grids, int box, float delt, float grav,
+    float re_equiv, float reynolds,
+    const float* grd_xmin, const float* grd_xmax, const float* grd_ymin,
+    const float* grd_ymax, const float* grd_zmin, const float* grd_zmax,
+    int isotropic);
+
+/* ---- a2: push_elec -- sub_push_elec.f90:4-5 (reads arg 1, writes arg 3) */
+int g3m3_push_elec(g3m3_ctx* ctx, const float* wrkepres,
+    const float* oldepres, float* epres, const float* evx, const float* evy,
+    const float* evz, float gamma, float gamma1, int nx, int ny, int nz,
+    int n_grids, int box, float delt, float rx, float ry, float rz);
+
+/* ---- a3: push_bfld -- sub_push_bfld.f90:4-6 --------------------------- */
+int g3m3_push_bfld(g3m3_ctx* ctx, float* bx, float* by, float* bz,
+    const float* oldbx, const float* oldby, const float* oldbz,
+    const float* efldx, const float* efldy, const float* efldz,
+    int nx, int ny, int nz, int n_grids, int box, float delt,
+    float rx, float ry, float rz);
+
+/* ---- a4: calcur -- sub_calcur.f90:5-6 --------------------------------- */
+int g3m3_calcur(g3m3_ctx* ctx, const float* bx, const float* by,
+    const float* bz, int nx, int ny, int nz, int n_grids, int box,
+    float* curx, float* cury, float* curz, float rx, float ry, float rz);
+
+/* bs = b0 + b, btot = max(|bs|, smallbit) of one box (3d_main.f90:2248-2254;
+ * an array statement of the main program, not a subroutine). */
+int g3m3_total_b(g3m3_ctx* ctx, const float* bx, const float* by,
+    const float* bz, const float* bx0, const float* by0, const float* bz0,
+    int nx, int ny, int nz, int n_grids, int box, float smallbit,
+    float* bsx, float* bsy, float* bsz, float* btot);
+
+/* ---- a5: fnd_evel -- sub_fnd_evel.f90:4-7; fnd_vtot -- sub_fnd_vtot.f90:4-6 */
+int g3m3_fnd_evel(g3m3_ctx* ctx, const float* qpx, const float* qpy,
+    const float* qpz, const float* qrho, const float* hpx, const float* hpy,
+    const float* hpz, const float* hrho, const float* opx, const float* opy,
+    const float* opz, const float* orho, const float* curx,
+    const float* cury, const float* curz, float* evx, float* evy,
+    float* evz, float* tvx, float* tvy, float* tvz,
+    int nx, int ny, int nz, int n_grids, int box,
+    float rmassq, float rmassh, float rmasso, float reynolds);
+
+int g3m3_fnd_vtot(g3m3_ctx* ctx, const float* qpx, const float* qpy,
+    const float* qpz, const float* qrho, const float* hpx, const float* hpy,
+    const float* hpz, const float* hrho, const float* opx, const float* opy,
+    const float* opz, const float* orho, float* vx, float* vy, float* vz,
+    int nx, int ny, int nz, int n_grids, int box,
+    float rmassq, float rmassh, float rmasso);
+
+/* ---- a6: BandE -- sub_BandE.f90:5-10 --------------------------------- */
+int g3m3_bande(g3m3_ctx* ctx, float* efldx, float* efldy, float* efldz,
+    const float* bsx, const float* bsy, const float* bsz,
+    const float* curx, const float* cury, const float* curz,
+    const float* evx, const float* evy, const float* evz, const float* btot,
+    const float* epres, const float* qrho, const float* hrho,
+    const float* orho, const float* rst, float resist, float reynolds,
+    int nx, int ny, int nz, int n_grids, int box,
+    float rmassq, float rmassh, float rmasso,
+    const int* ijmid, const int* nummid, const int* ijzero, int mbndry,
+    const int* numzero, int mmid, int mzero, float rx, float ry, float rz);
+
+/* ---- a7: fnd_pres -- sub_fnd_pres.f90:5-6 ---------------------------- */
+int g3m3_fnd_pres(g3m3_ctx* ctx, const float* px, const float* py,
+    const float* pz, const float* pxy, const float* pxz, const float* pyz,
+    float* p_para, float* p_perp, float* p_cross,
+    const float* vvx, const float* vvy, const float* vvz,
+    const float* bxt, const float* byt, const float* bzt,
+    int nx, int ny, int nz, int n_grids, int box);
+
+/* ---- a8: lap_plasma -- sub_lap_plasma.f90:4-10; lap_elec :151-152;
+ *          lap_bfld :202-203 ---------------------------------------------- */
+int g3m3_lap_plasma(g3m3_ctx* ctx, const float* rho, const float* px,
+    const float* py, const float* pz, const float* presx,
+    const float* presy, const float* presz, const float* presxy,
+    const float* presxz, const float* presyz,
+    float* wrkrho, float* wrkpx, float* wrkpy, float* wrkpz,
+    float* wrkpresx, float* wrkpresy, float* wrkpresz,
+    float* wrkpresxy, float* wrkpresxz, float* wrkpresyz,
+    const float* vx, const float* vy, const float* vz,
+    int nx, int ny, int nz, int n_grids, int box,
+    float chirho, float chipxyz, float chierg, float delt, int isotropic);
+
+int g3m3_lap_elec(g3m3_ctx* ctx, const float* ppres, float* wrkppres,
+    const float* vx, const float* vy, const float* vz,
+    int nx, int ny, int nz, int n_grids, int box,
+    float chirho, float chipxyz, float chierg, float delt);
+
+int g3m3_lap_bfld(g3m3_ctx* ctx, const float* bx, const float* by,
+    const float* bz, float* wrkbx, float* wrkby, float* wrkbz,
+    const float* vx, const float* vy, const float* vz,
+    int nx, int ny, int nz, int n_grids, int box,
+    float chirho, float chipxyz, float chierg, float delt);
+
+/* ---- a9: fcsmooth -- sub_fcsmooth.f90:7-8 (tempx..z are scratch) ------
+ *          flux_correct -- sub_flux_correct.f90:4-35, the 34 fields as
+ *          pointer tables in the field order of g3m3_types.h ------------- */
+int g3m3_fcsmooth(g3m3_ctx* ctx, float* px, const float* oldpx,
+    const float* wrkpx, int nx, int ny, int nz, int n_grids, int box,
+    float chipx, float* tempx, float* tempy, float* tempz);
+
+int g3m3_flux_correct(g3m3_ctx* ctx, float* const cur[G3M3_NFIELDS],
+    const float* const wrk[G3M3_NFIELDS], const float* const old[G3M3_NFIELDS],
+    int nx, int ny, int nz, int n_grids, int box, float difrho, float diferg);
+
+/* ---- a10: set_rho -- sub_set_rho.f90:5-11 ---------------------------- */
+int g3m3_set_rho(g3m3_ctx* ctx, float* qrho, float* qpresx, float* qpresy,
+    float* qpresz, float* qpresxy, float* qpresxz, float* qpresyz,
+    float rmassq, float* hrho, float* hpresx, float* hpresy, float* hpresz,
+    float* hpresxy, float* hpresxz, float* hpresyz, float rmassh,
+    float* orho, float* opresx, float* opresy, float* opresz,
+    float* opresxy, float* opresxz, float* opresyz, float rmasso,
+    float* epres, int nx, int ny, int nz, int n_grids, int box,
+    float o_conc);
+
+/* ---- a11: set_speed_agrd -- sub_set_speed_agrd.f90:6-22 --------------
+ * The six returned scalars are host pointers (the call synchronizes). */
+int g3m3_set_speed_agrd(g3m3_ctx* ctx, int nx, int ny, int nz,
+    int n_grids, int box, float rmassq, float rmassh, float rmasso,
+    int isotropic, float smallbit, float aniso_limit, float vlim,
+    float qvlim, float hvlim, float ovlim, float qclim, float hclim,
+    float oclim, float cslim,
+    const float* bx, const float* by, const float* bz,
+    const float* bx0, const float* by0, const float* bz0,
+    float* qrho, float* qpx, float* qpy, float* qpz,
+    float* qpresx, float* qpresy, float* qpresz,
+    float* qpresxy, float* qpresxz, float* qpresyz,
+    float* hrho, float* hpx, float* hpy, float* hpz,
+    float* hpresx, float* hpresy, float* hpresz,
+    float* hpresxy, float* hpresxz, float* hpresyz,
+    float* orho, float* opx, float* opy, float* opz,
+    float* opresx, float* opresy, float* opresz,
+    float* opresxy, float* opresxz, float* opresyz,
+    float* epres, float* btot,
+    float* pxmax, float* pymax, float* pzmax, float* csmax, float* alfmax,
+    float* fastest);
+
+/* ---- a12: store_array -- sub_store_array.f90:1 (writes argument 1) ---- */
+int g3m3_store_array(g3m3_ctx* ctx, float* bx, const float* bx0,
+    int nx, int ny, int nz, int n_grids, int box);
+
+/* ---- a13: bndry_outer -- sub_bndry_outer.f90:5-16 (34 fields as a table)
+ * ---- a14: bndry_inner -- sub_bndry_inner.f90:5-20 -------------------- */
+int g3m3_bndry_outer(g3m3_ctx* ctx, float* const f[G3M3_NFIELDS],
+    const float* bx0, const float* by0, const float* bz0,
+    const g3m3_params* p);
+
+int g3m3_bndry_inner(g3m3_ctx* ctx, float* const f[G3M3_NFIELDS],
+    const float* parm_srf, const float* parm_mid, const float* parm_zero,
+    const int* ijsrf, const int* numsrf, const int* ijmid,
+    const int* nummid, const int* ijzero, const int* numzero,
+    int msrf, int mmid, int mzero, const g3m3_params* p);
+
+/* ---- a15: flanks -- sub_flanks.f90:5-7; bndry_flanks (34 fields) -------
+ * t_new/t_old are the reference's real(dp) time arrays (host). */
+int g3m3_flanks(g3m3_ctx* ctx, float* wrkrho, const float* rho,
+    const float* oldrho, int nx, int ny, int nz, int n_grids, int box,
+    const double* t_new, const double* t_old, double t, float* work,
+    const float* grd_xmin, const float* grd_xmax, const float* grd_ymin,
+    const float* grd_ymax, const float* grd_zmin, const float* grd_zmax);
+
+int g3m3_bndry_flanks(g3m3_ctx* ctx, float* const target[G3M3_NFIELDS],
+    const float* const cur[G3M3_NFIELDS], const float* const old[G3M3_NFIELDS],
+    int nx, int ny, int nz, int n_grids, int box,
+    const double* t_old, const double* t_new, double t,
+    const float* grd_xmin, const float* grd_xmax, const float* grd_ymin,
+    const float* grd_ymax, const float* grd_zmin, const float* grd_zmax);
+
+/* ---- a16: corer -- sub_corer.f90:5-6; bndry_corer (34 fields) --------- */
+int g3m3_corer(g3m3_ctx* ctx, float* rho, int nx, int ny, int nz,
+    int n_grids, int box, const float* grd_xmin, const float* grd_xmax,
+    const float* grd_ymin, const float* grd_ymax, const float* grd_zmin,
+    const float* grd_zmax);
+
+int g3m3_bndry_corer(g3m3_ctx* ctx, float* const f[G3M3_NFIELDS],
+    int nx, int ny, int nz, int n_grids, int box,
+    const float* grd_xmin, const float* grd_xmax, const float* grd_ymin,
+    const float* grd_ymax, const float* grd_zmin, const float* grd_zmax);
+
+/* ---- a17: flanks_synced -- sub_flanks_synced.f90:5-6 ----------------- */
+int g3m3_flanks_synced(g3m3_ctx* ctx, float* rho, int nx, int ny, int nz,
+    int n_grids, int box, const float* grd_xmin, const float* grd_xmax,
+    const float* grd_ymin, const float* grd_ymax, const float* grd_zmin,
+    const float* grd_zmax);
+
+/* ---- a18: divB_correct -- sub_divB_correct.f90:25-27 (with its
+ * sparse_solver, sub_sparse_solver.f90:19-20).  The initial iterate is 0
+ * (the reference starts from uninitialised memory).  *iters (may be NULL)
+ * receives the CG iteration count; G3M3_ERR_NOCONV is returned (with the
+ * partially cleaned field written) when the solver stops without meeting
+ * its tolerance, which the reference only reports as a warning. */
+int g3m3_divb_correct(g3m3_ctx* ctx, int nx, int ny, int nz, int n_grids,
+    int box, int nbands, const int* divb_band_pos, const float* xspac,
+    float divb_errlim, float* bx, float* by, float* bz, int* iters);
+
+/* ---- a19: virtual spacecraft -- findgrid cft_findgrid.f90:4 and
+ * trilin_interp cft_trilin_interp.f90:10, batched over n trajectory points:
+ * xyz(3,n) in planet radii; out(n) = trilinear value of field at each point
+ * in the smallest box that contains it (the perturbation field, as
+ * cft_craft_handling.f90:178-189 samples it). */
+int g3m3_sample_points(g3m3_ctx* ctx, const float* field, int nx, int ny,
+    int nz, int n_grids, const float* grid_minvals, const float* grid_maxvals,
+    const float* xspac, float re_equiv, const float* xyz, int n, float* out);
+
+/* ---- a20: the step engine -------------------------------------------- */
+/* Create a model holding n_grids boxes of the given params on the device.
+ * Upload the state with g3m3_model_set_field (cur fields), the dipole with
+ * g3m3_model_set_b0 and the inner-boundary lists with
+ * g3m3_model_set_inner; then g3m3_model_init_steps. */
+int g3m3_model_create(g3m3_ctx* ctx, const g3m3_params* p, g3m3_model** out);
+int g3m3_model_destroy(g3m3_model* m);
+/* field: 0..33 (g3m3_types.h order); data: A(nx,ny,nz,n_grids), host or
+ * device.  which: 0 = current state, 1 = old, 2 = wrk copy. */
+int g3m3_model_set_field(g3m3_model* m, int which, int field, const float* data);
+int g3m3_model_get_field(g3m3_model* m, int which, int field, float* data);
+/* All 34 current fields at once from/to a host block of 34 contiguous
+ * A(nx,ny,nz,n_grids) arrays (one copy per direction). */
+int g3m3_model_set_state(g3m3_model* m, const float* data);
+int g3m3_model_get_state(g3m3_model* m, float* data);
+int g3m3_model_set_b0(g3m3_model* m, const float* bx0, const float* by0, const float* bz0);
+int g3m3_model_set_inner(g3m3_model* m, const float* resistive,
+    const int* ijsrf, const int* numsrf, const float* parm_srf, int msrf,
+    const int* ijmid, const int* nummid, const float* parm_mid, int mmid,
+    const int* ijzero, const int* numzero, const float* parm_zero, int mzero);
+/* Guards and first time steps, 3d_main.f90:1861-1903. */
+int g3m3_model_init_steps(g3m3_model* m);
+/* Run nsteps main steps.  use_graph: 0 = launch kernels from the host loop
+ * (plain), 1 = replay one captured CUDA graph per main step. */
+int g3m3_model_run(g3m3_model* m, int nsteps, int use_graph);
+/* div B cleaning of every box plus flanks_synced and bndry_corer
+ * (3d_main.f90:3363-3408). */
+int g3m3_model_divb_all(g3m3_model* m);
+/* Time bookkeeping: t, t_stepnew(1..n_grids), executed cell-updates. */
+int g3m3_model_times(g3m3_model* m, double* t, double* t_stepnew,
+    int64_t* cell_updates);
+/* Launch counters of the last g3m3_model_run (kernels, graph launches). */
+int g3m3_model_stats(g3m3_model* m, int64_t* kernels, int64_t* graphs);
+/* Stream of the model (for CUDA-event timing by the caller). */
+void* g3m3_model_stream(g3m3_model* m);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
