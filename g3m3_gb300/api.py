@@ -60,9 +60,13 @@ class Context:
             raise G3M3Error(rc, "context creation failed (no CUDA device?)")
         self.h = h
         self._keep = []
+        self._models = []
 
     def close(self):
         if self.h:
+            for m in list(self._models):   # models use the context's stream
+                m.close()
+            self._models = []
             self.L.g3m3_ctx_destroy(self.h)
             self.h = None
 
@@ -125,6 +129,7 @@ class Model:
         h = ctypes.c_void_p()
         ctx.check(self.L.g3m3_model_create(ctx.h, ctypes.byref(self.p), ctypes.byref(h)))
         self.h = h
+        ctx._models.append(self)
         self.upload(state)
 
     def upload(self, state):
@@ -192,9 +197,9 @@ class Model:
         return self.L.g3m3_model_stream(self.h)
 
     def close(self):
-        if self.h:
+        if self.h and self.ctx.h:
             self.L.g3m3_model_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:

@@ -22,6 +22,9 @@ LIB = os.path.join(OUT_DIR, "libg3m3_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
          "-ftz=false", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+         # host-side float arithmetic (time steps, geometry) must not be fused
+         # either: gcc contracts a*b+c into fma by default on aarch64
+         "-Xcompiler", "-ffp-contract=off",
          "-I", os.path.join(HERE, "..", "include")]
 
 

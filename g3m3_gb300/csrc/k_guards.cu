@@ -85,8 +85,8 @@ __global__ void __launch_bounds__(256) k_guards(const __grid_constant__ GuardArg
       const bool floored = a.do_set_rho && floor_sp(v, rmin[s]);
       newr[s] = v.r;
       if (floored && !a.do_speed) {   // no neighbour reads: store in place
-        const int b = 10 * s;
-        a.f[b + 0][c] = v.r; a.f[b + 1][c] = v.px; a.f[b + 2][c] = v.py; a.f[b + 3][c] = v.pz;
+        const int b = 10 * s;         // (set_rho leaves the momenta alone)
+        a.f[b + 0][c] = v.r;
         a.f[b + 4][c] = v.xx; a.f[b + 5][c] = v.yy; a.f[b + 6][c] = v.zz;
         a.f[b + 7][c] = v.xy; a.f[b + 8][c] = v.xz; a.f[b + 9][c] = v.yz;
         continue;
