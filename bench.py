@@ -1,0 +1,307 @@
+"""Benchmark of the G3M^3 multifluid step on GB300.
+
+Workload (default): the production nested grid -- 5 boxes of 121x121x61,
+2x refined, FP32 state, 34 fields per box, sub-cycled (box b steps up to
+2^(5-b) times per main step), div B cleaning every 10 main steps.  A "step"
+is one main step of the reference time loop (3d_main.f90:1925-3095).
+Metric: multifluid cell-updates/s (cells x executed box-steps / time).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the reference step on the
+host cores (OpenMP, every host thread): the reference itself is Fortran and
+no Fortran compiler exists in this image, so its restatement stands in.
+With N>1 (torchrun) every rank advances its own replica: the path has no
+data exchange between members.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "multifluid cell-updates/s"
+WORKLOAD = "nested grid, 5 boxes 121x121x61, 2x refinement, sub-cycled, FP32, divB CG every 10 steps"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------ our arm
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    from g3m3_gb300.api import Context, Model, addr
+    from g3m3_gb300.state import make_config
+
+    st = make_config("nested", seed=20261203 + rank)
+    p = st.params
+    ctx = Context(local)
+    m = Model(ctx, st)
+    m.init_steps()
+    stream = torch.cuda.ExternalStream(m.stream)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+
+    def timed(nsteps, graph):
+        t0c, _, cu0 = m.times()
+        k0 = 0
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        barrier()
+        e0.record(stream)
+        m.run(nsteps, graph=graph)
+        e1.record(stream)
+        barrier()
+        ms = e0.elapsed_time(e1)
+        _, tsn, cu1 = m.times()
+        k, g = m.stats()
+        return ms, cu1 - cu0, k
+
+    # warm-up (captures the graphs for the schedule shapes seen)
+    m.run(max(args.warmup, 3), graph=True)
+    m.run(1, graph=False)
+    clocks = Clocks(local)
+    clocks.start()
+    ms_g, cu_g, k_g = timed(args.steps, True)
+    clk = clocks.stop()
+    ms_p, cu_p, k_p = timed(max(2, args.steps // 2), False)
+
+    # e2e: state from pinned host memory every step, result read back
+    n4 = p.n_grids * p.nz * p.ny * p.nx
+    host = torch.empty((34 * n4,), dtype=torch.float32, pin_memory=True)
+    host_np = host.numpy()
+    m.state(out=host_np.reshape(34, p.n_grids, p.nz, p.ny, p.nx))
+    e2e_steps = max(2, args.steps // 2)
+    barrier()
+    t0 = time.perf_counter()
+    cu_e0 = m.times()[2]
+    for _ in range(e2e_steps):
+        m.set_state(host_np)
+        m.run(1, graph=True)
+        m.state(out=host_np.reshape(34, p.n_grids, p.nz, p.ny, p.nx))
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    cu_e = m.times()[2] - cu_e0
+
+    # per-kernel times (CUDA events on the engine's stream) for the roofline;
+    # this overwrites the wrk/old copies, so it runs after the timed legs
+    rows = kernel_table(m)
+    roof = roofline_from(rows)
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms_g, ms_p, e2e_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_g, ms_p, e2e_s = (float(x) for x in t.tolist())
+    m.close()
+    ctx.close()
+    if rank != 0:
+        return None
+    value = ws * cu_g / (ms_g / 1e3)
+    line = {
+        "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_g / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded state from the "
+        "reference's initial-condition formulas + 1% noise)",
+        "config": {"workload": WORKLOAD, "boxes": p.n_grids, "box": [p.nx, p.ny, p.nz],
+                   "cells_per_box": p.nx * p.ny * p.nz, "cell_updates_per_step": cu_g / args.steps,
+                   "mode": "one CUDA graph per main step", "l2": "working set (>400 MB per box) exceeds L2",
+                   "parallelism": f"replicas x{ws}"},
+        "plain": {"value": ws * cu_p / (ms_p / 1e3), "ms_per_step": ms_p / max(2, args.steps // 2),
+                  "mode": "kernels launched from the host loop"},
+        "e2e": {"value": ws * cu_e / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": 34 * n4 * 4,
+                "d2h_bytes_per_step": 34 * n4 * 4,
+                "path": "g3m3_model_set_state (pinned host) + g3m3_model_run(1 step) + g3m3_model_get_state"},
+        "gpu_launches": int(k_g),
+        "roofline": roof,
+        "kernels": rows,
+        "clocks": clk,
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline()
+    return line
+
+
+KERNELS = {  # id: (name, launches per box-step)
+    0: ("push_ion", 6), 1: ("fcsmooth x34", 1), 2: ("set_rho+set_speed_agrd", 4),
+    3: ("lapidus (10 fields)", 3), 4: ("flanks x34", 4), 5: ("calcur+bs/btot", 2), 6: ("BandE", 2),
+}
+
+
+def kernel_table(m, reps=20):
+    """Each engine kernel on box 1 of the nested grid, CUDA events on the
+    engine's stream; share = launches per box-step x time per launch."""
+    import ctypes
+    rows = {}
+    for kid, (name, per_step) in KERNELS.items():
+        ms = ctypes.c_float()
+        by = ctypes.c_double()
+        rc = m.L.g3m3_model_time_kernel(m.h, kid, 1, reps, ctypes.byref(ms), ctypes.byref(by))
+        if rc:
+            continue
+        rows[name] = {"ms_per_launch": ms.value, "launches_per_box_step": per_step,
+                      "algorithmic_bytes_per_launch": by.value,
+                      "achieved_gbs": by.value / (ms.value / 1e3) / 1e9}
+    tot = sum(r["ms_per_launch"] * r["launches_per_box_step"] for r in rows.values())
+    for r in rows.values():
+        r["share_of_timed_kernels"] = r["ms_per_launch"] * r["launches_per_box_step"] / tot if tot else None
+    return rows
+
+
+def roofline_from(rows):
+    name = max(rows, key=lambda k: rows[k]["ms_per_launch"] * rows[k]["launches_per_box_step"])
+    r = rows[name]
+    peak, kind = peaks()
+    return {"kernel": name + " (121x121x61 box)", "bound": "hbm", "achieved": r["achieved_gbs"], "peak": peak,
+            "unit": "GB/s", "frac": r["achieved_gbs"] / peak, "peak_source": kind,
+            "ms_per_launch": r["ms_per_launch"], "algorithmic_bytes_per_launch": r["algorithmic_bytes_per_launch"],
+            "traffic": None}
+
+
+def cpu_baseline(max_seconds: float = 25.0):
+    """The CPU restatement (OpenMP, all host threads) on a bounded sample:
+    main steps of the same nested grid until ~max_seconds have passed."""
+    from g3m3_gb300.state import make_config
+    from oracle.oracle import OracleModel
+    st = make_config("nested", divb_every=0)
+    om = OracleModel(st, omp=True)
+    om.init_steps()
+    t0 = time.perf_counter()
+    n = 0
+    cu0 = om.cell_updates
+    while True:
+        om.main_step()
+        n += 1
+        if time.perf_counter() - t0 > max_seconds or n >= 3:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": (om.cell_updates - cu0) / dt, "unit": "cell-updates/s", "cores": os.cpu_count(),
+            "kind": "port", "sample": f"{n} main step(s) of the nested 5-box grid (no divB), OpenMP"}
+
+
+# ------------------------------------------------------------ reference arm
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return None
+    from g3m3_gb300.state import make_config
+    from oracle.oracle import OracleModel
+    st = make_config("nested", divb_every=0)
+    om = OracleModel(st, omp=True)
+    om.init_steps()
+    steps = min(args.steps, 2)
+    for _ in range(min(args.warmup, 1)):
+        om.main_step()
+    cu0 = om.cell_updates
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        om.main_step()
+    dt = time.perf_counter() - t0
+    v = (om.cell_updates - cu0) / dt
+    sample = f"{steps} main step(s) of the nested 5-box grid after {min(args.warmup, 1)} warm-up (no divB)"
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": "cell-updates/s", "n_gpus": ws,
+            "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": dt / steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "parallelism": "host OpenMP"},
+            "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "CPU restatement of the Fortran reference (no Fortran compiler in the image)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    line = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

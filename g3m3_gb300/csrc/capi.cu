@@ -223,6 +223,8 @@ const char* g3m3_version(void) {
   return "g3m3_gpu sm_103a; FP32 state, IEEE div/sqrt, no FMA contraction; FP64 CG reductions";
 }
 
+void* g3m3_ctx_stream(g3m3_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
 int g3m3_ctx_create(g3m3_ctx** out, int device) {
   if (!out) return G3M3_ERR_ARG;
   *out = nullptr;

@@ -841,6 +841,116 @@ int g3m3_model_run(g3m3_model* m, int nsteps, int use_graph) {
   return G3M3_OK;
 }
 
+int g3m3_model_time_kernel(g3m3_model* m, int kernel, int box, int reps, float* ms_per_launch, double* bytes) {
+  if (!m || box < 1 || box > m->p.n_grids || reps < 1 || !ms_per_launch) return G3M3_ERR_ARG;
+  const g3m3_params& p = m->p;
+  const int b = box;
+  const size_t n3 = m->n3;
+  const size_t inner = (size_t)(m->d.nx - 2) * (m->d.ny - 2) * (m->d.nz - 2);
+  const int slot = scal_slot(m, 0.01f);
+  m->nscal = 0;
+  if (slot < 0) return G3M3_ERR_STATE;
+  cudaStream_t s = S(m);
+  cudaError_t e = cudaMemcpyAsync(m->d_scal, m->h_scal, sizeof(float), cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_check(m->ctx, e, "time_kernel");
+  double by = 0.0;
+  auto launch = [&]() -> int {
+    switch (kernel) {
+      case 0: {  // corrector-form push of species q: src = cur, out = wrk
+        PushIonArgs a{};
+        for (int f = 0; f < 10; f++) { a.out[f] = W(m, f, b); a.old[f] = O(m, f, b); a.src[f] = C(m, f, b); }
+        for (int q = 0; q < 3; q++) { a.bs[q] = m->bs[q]; a.efld[q] = m->efld[q]; a.tv[q] = m->tv[q]; }
+        a.btot = m->btot; a.d = m->d;
+        a.g.xmin = p.grd_xmin[b - 1]; a.g.ymin = p.grd_ymin[b - 1]; a.g.zmin = p.grd_zmin[b - 1];
+        a.g.dx = (p.grd_xmax[b - 1] - p.grd_xmin[b - 1]) / (float)(m->d.nx - 1);
+        a.g.dy = (p.grd_ymax[b - 1] - p.grd_ymin[b - 1]) / (float)(m->d.ny - 1);
+        a.g.dz = (p.grd_zmax[b - 1] - p.grd_zmin[b - 1]) / (float)(m->d.nz - 1);
+        a.rmass = p.rmassq; a.grav = p.grav; a.re_equiv = p.re_equiv; a.reynolds = p.reynolds;
+        a.delt = sref(m, slot); a.boundary_from_old = 0;
+        launch_push_ion(a, s);
+        by = 160.0 * inner;     // 30 arrays read, 10 written per interior cell
+        return 0;
+      }
+      case 1: {
+        FcsArgs fa{};
+        for (int q = 0; q < G3M3_NFIELDS; q++) {
+          fa.px[q] = O(m, q, b); fa.old[q] = C(m, q, b); fa.wrk[q] = W(m, q, b);
+          fa.chi[q] = q >= G3M3_F_BX ? p.diferg : p.difrho;
+        }
+        fa.nf = G3M3_NFIELDS; fa.d = m->d;
+        launch_fcsmooth(fa, s);
+        by = 12.0 * G3M3_NFIELDS * n3;   // wrk, old read, result written, per field
+        return 0;
+      }
+      case 2: {
+        int st = guard_stage(m, W, b, true, false);
+        by = (37.0 + 2.0) * 4.0 * n3;    // 30 species + epres + b + b0 read; btot, epres written
+        return st;
+      }
+      case 3: {
+        LapArgs la{};
+        for (int f = 0; f < 10; f++) { la.in[f] = C(m, f, b); la.out[f] = W(m, f, b); la.chi[f] = 0.1f; }
+        la.nf = 10;
+        for (int q = 0; q < 3; q++) la.vp[q] = C(m, 1 + q, b);
+        la.vrho = C(m, 0, b); la.vfloor = p.smallbit; la.d = m->d; la.delt = sref(m, slot);
+        launch_lap(la, s);
+        by = 80.0 * inner;
+        return 0;
+      }
+      case 4: {
+        if (b >= p.n_grids) return G3M3_ERR_ARG;
+        FlanksArgs a{};
+        for (int q = 0; q < G3M3_NFIELDS; q++) { a.target[q] = W(m, q, b); a.curc[q] = C(m, q, b + 1); a.oldc[q] = O(m, q, b + 1); }
+        a.nf = G3M3_NFIELDS;
+        fill_flanks_geometry(a, m->d.nx, m->d.ny, m->d.nz, b, p.grd_xmin, p.grd_xmax, p.grd_ymin, p.grd_ymax, p.grd_zmin, p.grd_zmax);
+        a.t1 = sref(m, slot);
+        launch_flanks(a, s);
+        by = 8.0 * G3M3_NFIELDS * (double)shell_count(m->d, 2);   // shell read-modify-write
+        return 0;
+      }
+      case 5: {
+        CurrentArgs ca{};
+        for (int q = 0; q < 3; q++) { ca.b[q] = C(m, G3M3_F_BX + q, b); ca.b0[q] = m->b0[q] + (size_t)(b - 1) * n3; ca.cur[q] = m->curr[q]; ca.bs[q] = m->bs[q]; }
+        ca.btot = m->btot; ca.d = m->d;
+        ca.rx = ca.ry = ca.rz = p.xspac[b - 1]; ca.smallbit = p.smallbit;
+        launch_current(ca, s);
+        by = 52.0 * n3;
+        return 0;
+      }
+      case 6: {
+        BandEArgs ba{};
+        for (int q = 0; q < 3; q++) { ba.efld[q] = m->efld[q]; ba.bs[q] = m->bs[q]; ba.cur[q] = m->curr[q]; ba.ev[q] = m->ev[q]; ba.rho[q] = C(m, 10 * q, b); }
+        ba.epres = C(m, G3M3_F_EPRES, b); ba.rst_e = nullptr; ba.d = m->d;
+        ba.rmass[0] = p.rmassq; ba.rmass[1] = p.rmassh; ba.rmass[2] = p.rmasso;
+        ba.reynolds = p.reynolds; ba.rx = ba.ry = ba.rz = p.xspac[b - 1];
+        launch_bande(ba, s);
+        by = 52.0 * n3;
+        return 0;
+      }
+      default:
+        return G3M3_ERR_ARG;
+    }
+  };
+  int st = launch();   // warm-up
+  if (st) return st;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, s);
+  for (int r = 0; r < reps && !st; r++) st = launch();
+  cudaEventRecord(e1, s);
+  e = cudaEventSynchronize(e1);
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  if (e != cudaSuccess) return cuda_check(m->ctx, e, "time_kernel");
+  *ms_per_launch = ms / (float)reps;
+  if (bytes) *bytes = by;
+  return G3M3_OK;
+}
+
 int g3m3_model_times(g3m3_model* m, double* t, double* t_stepnew, int64_t* cell_updates) {
   if (!m) return G3M3_ERR_ARG;
   if (t) *t = m->t;

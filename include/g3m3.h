@@ -66,6 +66,8 @@ int g3m3_release_mirrors(g3m3_ctx* ctx);
 int g3m3_synchronize(g3m3_ctx* ctx);
 /* Library build description (kernel arch, flags). */
 const char* g3m3_version(void);
+/* The context's CUDA stream (cudaStream_t), for event timing by callers. */
+void* g3m3_ctx_stream(g3m3_ctx* ctx);
 
 /* ---- a1: push_ion -- sub_push_ion.f90:4-17 ---------------------------- */
 int g3m3_push_ion(g3m3_ctx* ctx,
@@ -322,6 +324,15 @@ int g3m3_model_times(g3m3_model* m, double* t, double* t_stepnew,
 int g3m3_model_stats(g3m3_model* m, int64_t* kernels, int64_t* graphs);
 /* Stream of the model (for CUDA-event timing by the caller). */
 void* g3m3_model_stream(g3m3_model* m);
+/* Measurement hook: launch one kernel of the engine `reps` times on box
+ * `box` of the model, timed with CUDA events on the model's stream.
+ * kernel: 0 push_ion (one species), 1 fcsmooth (34 fields), 2 set_rho +
+ * set_speed_agrd pass, 3 Lapidus (one species, 10 fields), 4 flanks (34
+ * fields, box < n_grids), 5 calcur + bs/btot, 6 BandE.  Outputs go to the
+ * wrk/old copies, so call it only between runs whose state no longer
+ * matters.  *bytes receives the algorithmic bytes of one launch. */
+int g3m3_model_time_kernel(g3m3_model* m, int kernel, int box, int reps,
+    float* ms_per_launch, double* bytes);
 
 #ifdef __cplusplus
 }
