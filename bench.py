@@ -290,6 +290,21 @@ def run_reference(args):
             "note": "CPU restatement of the Fortran reference (no Fortran compiler in the image)"}
 
 
+def run_profile(args):
+    """A single 121x121x61 box (state > L2, < 1 GB on the device) stepped with
+    host-loop launches; used as the small case of the ncu captures."""
+    from g3m3_gb300.api import Context, Model
+    from g3m3_gb300.state import make_config
+    st = make_config("nested", n_grids=1, divb_every=0)
+    with Context(0) as ctx:
+        m = Model(ctx, st)
+        m.init_steps()
+        m.run(args.warmup + args.steps, graph=False)
+        k, _ = m.stats()
+        print(json.dumps({"profile_case": "1 box 121x121x61", "main_steps": args.warmup + args.steps,
+                          "kernel_launches": k}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -297,7 +312,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--profile", action="store_true",
+                    help="profiling case for ncu: one 121x121x61 box, warmup+steps main steps, host-loop launches")
     args = ap.parse_args()
+    if args.profile:
+        return run_profile(args)
     line = run_reference(args) if args.impl == "reference" else run_ours(args)
     if line is not None:
         print(json.dumps(line), flush=True)
