@@ -37,6 +37,19 @@ __device__ __forceinline__ Sp load_sp(const GuardArgs& a, int s, size_t c) {
   return v;
 }
 
+// the seven values the checks read; the off-diagonal pressures are loaded
+// only for a cell whose values are rewritten
+__device__ __forceinline__ Sp load_diag(const GuardArgs& a, int s, size_t c) {
+  const int b = 10 * s;
+  Sp v;
+  v.r = a.f[b + 0][c]; v.px = a.f[b + 1][c]; v.py = a.f[b + 2][c]; v.pz = a.f[b + 3][c];
+  v.xx = a.f[b + 4][c]; v.yy = a.f[b + 5][c]; v.zz = a.f[b + 6][c];
+  v.xy = 0.0f; v.xz = 0.0f; v.yz = 0.0f;
+  return v;
+}
+
+__device__ __forceinline__ float rho_min(int s) { return s == 0 ? 2.e-4f : (s == 1 ? 1.e-4f : 2.e-5f); }
+
 // set_rho for one species; returns true when the values changed
 __device__ __forceinline__ bool floor_sp(Sp& v, float rmin) {
   if (v.r < rmin || v.xx < 0.0f || v.yy < 0.0f || v.zz < 0.0f) {
@@ -72,22 +85,34 @@ __global__ void __launch_bounds__(256) k_guards(const __grid_constant__ GuardArg
   const int k = blockIdx.z * blockDim.z + threadIdx.z + 1;
   const bool inside = i <= d.nx && j <= d.ny && k <= d.nz;
   float mx = 0.0f, my = 0.0f, mz = 0.0f, mc = 0.0f, ma = 0.0f;
-  const float rmin[3] = {2.e-4f, 1.e-4f, 2.e-5f};
   if (inside) {
     const size_t c = d.at(i, j, k);
     const bool interior = i > 1 && j > 1 && k > 1 && i < d.nx && j < d.ny && k < d.nz;
     float newr[3];
+    Sp sp3[3];   // every species value of this cell, loaded before any store
+#pragma unroll
+    for (int s = 0; s < 3; s++) sp3[s] = load_diag(a, s, c);
+    float bsum[3] = {0.0f, 0.0f, 0.0f};
+    if (a.do_speed) {
+      bsum[0] = __ldg(a.b0[0] + c) + a.f[G3M3_F_BX][c];
+      bsum[1] = __ldg(a.b0[1] + c) + a.f[G3M3_F_BY][c];
+      bsum[2] = __ldg(a.b0[2] + c) + a.f[G3M3_F_BZ][c];
+    }
     float ep = a.f[G3M3_F_EPRES][c];
     if (a.do_set_rho) ep = fabsf(ep);
     bool ep_changed = a.do_set_rho;
+#pragma unroll
     for (int s = 0; s < 3; s++) {
-      Sp v = load_sp(a, s, c);
-      const bool floored = a.do_set_rho && floor_sp(v, rmin[s]);
+      Sp v = sp3[s];
+      // set_rho zeroes the off-diagonal terms of a repaired cell, so they
+      // matter only when the cell is limited without being repaired
+      const bool floored = a.do_set_rho && floor_sp(v, rho_min(s));
       newr[s] = v.r;
       if (floored && !a.do_speed) {   // no neighbour reads: store in place
         const int b = 10 * s;         // (set_rho leaves the momenta alone)
         a.f[b + 0][c] = v.r;
         a.f[b + 4][c] = v.xx; a.f[b + 5][c] = v.yy; a.f[b + 6][c] = v.zz;
+        a.f[b + 7][c] = 0.0f; a.f[b + 8][c] = 0.0f; a.f[b + 9][c] = 0.0f;
         a.f[b + 7][c] = v.xy; a.f[b + 8][c] = v.xz; a.f[b + 9][c] = v.yz;
         continue;
       }
@@ -110,7 +135,7 @@ __global__ void __launch_bounds__(256) k_guards(const __grid_constant__ GuardArg
         for (int q = 0; q < 10; q++) acc[q] = 0.0f;
         for (int m = 0; m < 6; m++) {
           Sp u = load_sp(a, s, nb[m]);
-          if (a.do_set_rho) floor_sp(u, rmin[s]);
+          if (a.do_set_rho) floor_sp(u, rho_min(s));
           float sx, sy, sz, sxy, sxz, syz;
           if (a.isotropic) {
             sx = u.xx; sy = u.xx; sz = u.xx; sxy = 0.0f; sxz = 0.0f; syz = 0.0f;
@@ -146,9 +171,7 @@ __global__ void __launch_bounds__(256) k_guards(const __grid_constant__ GuardArg
       mx = amax1(mx, avx); my = amax1(my, avy); mz = amax1(mz, avz); mc = amax1(mc, cq);
     }
     if (a.do_speed) {
-      const float sx = __ldg(a.b0[0] + c) + a.f[G3M3_F_BX][c];
-      const float sy = __ldg(a.b0[1] + c) + a.f[G3M3_F_BY][c];
-      const float sz = __ldg(a.b0[2] + c) + a.f[G3M3_F_BZ][c];
+      const float sx = bsum[0], sy = bsum[1], sz = bsum[2];
       const float bt = amax1(sqrtf(sx * sx + sy * sy + sz * sz), a.smallbit);
       a.btot[c] = bt;
       if (interior) {

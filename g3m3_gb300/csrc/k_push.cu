@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(256) k_push_ion(const __grid_constant__ PushIo
   };
 
   // continuity
-  a.out[0][c] = __ldg(a.old[0] + c) - delt * ((DV(__ldg(Px + xp) - __ldg(Px + xm), dxt, rdx)
+  const float o_rho = __ldg(a.old[0] + c) - delt * ((DV(__ldg(Px + xp) - __ldg(Px + xm), dxt, rdx)
                                                + DV(__ldg(Py + yp) - __ldg(Py + ym), dyt, rdy))
                                               + DV(__ldg(Pz + zp) - __ldg(Pz + zm), dzt, rdz));
   const float aqpx = __ldg(a.old[1] + c) - delt * fluxdiv(Px);
@@ -118,9 +118,9 @@ __global__ void __launch_bounds__(256) k_push_ion(const __grid_constant__ PushIo
   const float radius = sqrtf(ax * ax + ay * ay + az * az) + 0.0000001f;
   const float rr = a.re_equiv * radius;
   const float g = delt * rho_c * a.grav / (rr * rr);
-  a.out[1][c] = npx - g * ax / radius;
-  a.out[2][c] = npy - g * ay / radius;
-  a.out[3][c] = npz - g * az / radius;
+  const float o_px = npx - g * ax / radius;
+  const float o_py = npy - g * ay / radius;
+  const float o_pz = npz - g * az / radius;
 
   const float wx = __ldg(Wx + c), wy = __ldg(Wy + c), wz = __ldg(Wz + c);
   const float wxy = __ldg(Wxy + c), wxz = __ldg(Wxz + c), wyz = __ldg(Wyz + c);
@@ -140,17 +140,18 @@ __global__ void __launch_bounds__(256) k_push_ion(const __grid_constant__ PushIo
   float skin = rey;
   if (bmag > bmax) skin = rey * (bmax / bmag);
   const float gy2 = t2 * skin / a.rmass;
-  a.out[4][c] = px_ - DV(t2 * wxy * (vyp.x - vym.x), dyt, rdy) - DV(t2 * wxz * (vzp.x - vzm.x), dzt, rdz)
+  const float o_xx = px_ - DV(t2 * wxy * (vyp.x - vym.x), dyt, rdy) - DV(t2 * wxz * (vzp.x - vzm.x), dzt, rdz)
                 + gy2 * (wxy * abz - wxz * aby);
-  a.out[5][c] = py_ - DV(t2 * wxy * (vxp.y - vxm.y), dxt, rdx) - DV(t2 * wyz * (vzp.y - vzm.y), dzt, rdz)
+  const float o_yy = py_ - DV(t2 * wxy * (vxp.y - vxm.y), dxt, rdx) - DV(t2 * wyz * (vzp.y - vzm.y), dzt, rdz)
                 + gy2 * (wyz * abx - wxy * abz);
-  a.out[6][c] = pz_ - DV(t2 * wxz * (vxp.z - vxm.z), dxt, rdx) - DV(t2 * wyz * (vyp.z - vym.z), dyt, rdy)
+  const float o_zz = pz_ - DV(t2 * wxz * (vxp.z - vxm.z), dxt, rdx) - DV(t2 * wyz * (vyp.z - vym.z), dyt, rdy)
                 + gy2 * (wxz * aby - wyz * abx);
 
   const float gy1 = delt * skin / a.rmass;
+  float o_xy, o_xz, o_yz;
   {
     const float p0 = __ldg(a.old[7] + c) - delt * fluxdiv(Wxy);
-    a.out[7][c] = p0 - delt * wxy * (DV(vxp.x - vxm.x, dxt, rdx) + DV(vyp.y - vym.y, dyt, rdy))
+    o_xy = p0 - delt * wxy * (DV(vxp.x - vxm.x, dxt, rdx) + DV(vyp.y - vym.y, dyt, rdy))
                   - DV(delt * wy * (vyp.x - vym.x), dyt, rdy)
                   - DV(delt * wx * (vxp.y - vxm.y), dxt, rdx)
                   - DV(delt * wyz * (vzp.x - vzm.x), dzt, rdz)
@@ -159,7 +160,7 @@ __global__ void __launch_bounds__(256) k_push_ion(const __grid_constant__ PushIo
   }
   {
     const float p0 = __ldg(a.old[8] + c) - delt * fluxdiv(Wxz);
-    a.out[8][c] = p0 - delt * wxz * (DV(vxp.x - vxm.x, dxt, rdx) + DV(vzp.z - vzm.z, dzt, rdz))
+    o_xz = p0 - delt * wxz * (DV(vxp.x - vxm.x, dxt, rdx) + DV(vzp.z - vzm.z, dzt, rdz))
                   - DV(delt * wz * (vzp.x - vzm.x), dzt, rdz)
                   - DV(delt * wx * (vxp.z - vxm.z), dxt, rdx)
                   - DV(delt * wyz * (vyp.x - vym.x), dyt, rdy)
@@ -168,13 +169,18 @@ __global__ void __launch_bounds__(256) k_push_ion(const __grid_constant__ PushIo
   }
   {
     const float p0 = __ldg(a.old[9] + c) - delt * fluxdiv(Wyz);
-    a.out[9][c] = p0 - delt * wyz * (DV(vyp.y - vym.y, dyt, rdy) + DV(vzp.z - vzm.z, dzt, rdz))
+    o_yz = p0 - delt * wyz * (DV(vyp.y - vym.y, dyt, rdy) + DV(vzp.z - vzm.z, dzt, rdz))
                   - DV(delt * wy * (vyp.z - vym.z), dyt, rdy)
                   - DV(delt * wz * (vzp.y - vzm.y), dzt, rdz)
                   - DV(delt * wxy * (vxp.z - vxm.z), dxt, rdx)
                   - DV(delt * wxz * (vxp.y - vxm.y), dxt, rdx)
                   + gy1 * (abx * (wz - wy) - abz * wxz + aby * wxy);
   }
+  // every load above precedes every store: the output arrays are distinct
+  // from the inputs, but the compiler cannot know it through the tables
+  a.out[0][c] = o_rho; a.out[1][c] = o_px; a.out[2][c] = o_py; a.out[3][c] = o_pz;
+  a.out[4][c] = o_xx; a.out[5][c] = o_yy; a.out[6][c] = o_zz;
+  a.out[7][c] = o_xy; a.out[8][c] = o_xz; a.out[9][c] = o_yz;
 #undef DV
 }
 

@@ -140,7 +140,13 @@ void launch_vtot(const VtotArgs& a, cudaStream_t s) {
   k_vtot<<<blocks_for(a.d.cells(), 256), 256, 0, s>>>(a);
 }
 
-void launch_fcsmooth(const FcsArgs& a, cudaStream_t s) {
+void launch_fcsmooth_tiled(const FcsArgs& a, cudaStream_t s);
+
+void launch_fcsmooth(const FcsArgs& a, cudaStream_t s) { launch_fcsmooth_tiled(a, s); }
+
+// One thread per cell re-deriving every intermediate: kept as the simple
+// statement of the algorithm (not launched by the library).
+void launch_fcsmooth_percell(const FcsArgs& a, cudaStream_t s) {
   const dim3 blk(32, 4, 2);
   const unsigned kt = (unsigned)((a.d.nz + blk.z - 1) / blk.z);
   const dim3 grd((unsigned)((a.d.nx + blk.x - 1) / blk.x), (unsigned)((a.d.ny + blk.y - 1) / blk.y),
