@@ -29,6 +29,7 @@ struct FlanksArgs {         // fine box shell from the time-interpolated coarse 
   const float* curc[G3M3_NFIELDS];
   const float* oldc[G3M3_NFIELDS];
   int nf;
+  int fields_per_block;     // set by the launcher
   Dims d;
   ScalarRef t1;             // (t_new(mb)-t)/(t_new(mb)-t_old(mb)) rounded to FP32
   float sxmin, symin, szmin, sx, sy, sz;        // fine box

@@ -227,8 +227,9 @@ __device__ __forceinline__ Axis flank_axis(float smin, float sp, int idx, float 
 }
 
 __global__ void __launch_bounds__(256) k_flanks(const __grid_constant__ FlanksArgs a) {
+  // one thread per shell cell; the interpolation geometry is shared by all
+  // fields, which the thread then walks (blockIdx.y splits the field list)
   const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  const int f = blockIdx.y;
   int is, js, ks;
   const Dims d = a.d;
   if (!shell_cell(t, 2, d, is, js, ks)) return;
@@ -240,32 +241,40 @@ __global__ void __launch_bounds__(256) k_flanks(const __grid_constant__ FlanksAr
   if (X.b < 1 || Y.b < 1 || Z.b < 1 || X.b1 > d.nx || Y.b1 > d.ny || Z.b1 > d.nz) return;
   const float t1 = a.t1.get();
   const float t2 = 1.0f - t1;
-  const float* __restrict__ oc = a.oldc[f];
-  const float* __restrict__ cc = a.curc[f];
-  auto work = [&](int i, int j, int k) {
-    const size_t c = d.at(i, j, k);
-    return __ldg(oc + c) * t1 + __ldg(cc + c) * t2;
-  };
-  const float I = work(X.b, Y.b, Z.b) * X.dd * Y.dd * Z.dd + work(X.b, Y.b, Z.b1) * X.dd * Y.dd * Z.d
-                  + work(X.b, Y.b1, Z.b) * X.dd * Y.d * Z.dd + work(X.b, Y.b1, Z.b1) * X.dd * Y.d * Z.d
-                  + work(X.b1, Y.b, Z.b) * X.d * Y.dd * Z.dd + work(X.b1, Y.b, Z.b1) * X.d * Y.dd * Z.d
-                  + work(X.b1, Y.b1, Z.b) * X.d * Y.d * Z.dd + work(X.b1, Y.b1, Z.b1) * X.d * Y.d * Z.d;
+  const size_t c000 = d.at(X.b, Y.b, Z.b);
+  const size_t sx = 1, sy = (size_t)d.nx, sz = (size_t)d.nx * d.ny;
+  const size_t off[8] = {0, sz, sy, sy + sz, sx, sx + sz, sx + sy, sx + sy + sz};
+  // trilinear weights in the reference's term order (sub_flanks.f90:75-83)
+  const float wgt[8][3] = {{X.dd, Y.dd, Z.dd}, {X.dd, Y.dd, Z.d}, {X.dd, Y.d, Z.dd}, {X.dd, Y.d, Z.d},
+                           {X.d, Y.dd, Z.dd},  {X.d, Y.dd, Z.d},  {X.d, Y.d, Z.dd},  {X.d, Y.d, Z.d}};
   const size_t c = d.at(is, js, ks);
-  float w = a.target[f][c];
-  // panels in the reference's order: bottom, top, front, back, left, right;
-  // the inner layer blends half and half, the outer layer takes I
-  auto apply = [&](int layer) {
-    const float frac = (float)(layer - 1) / 2.0f;
-    const float frac1 = 1.0f - frac;
-    w = frac * w + frac1 * I;
-  };
-  if (ks <= 2) apply(ks);
-  if (ks >= d.nz - 1) apply(d.nz - ks + 1);
-  if (js <= 2) apply(js);
-  if (js >= d.ny - 1) apply(d.ny - js + 1);
-  if (is <= 2) apply(is);
-  if (is >= d.nx - 1) apply(d.nx - is + 1);
-  a.target[f][c] = w;
+  const int f_lo = blockIdx.y * a.fields_per_block;
+  const int f_hi = min(a.nf, f_lo + a.fields_per_block);
+  for (int f = f_lo; f < f_hi; f++) {
+    const float* __restrict__ oc = a.oldc[f];
+    const float* __restrict__ cc = a.curc[f];
+    float wk[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) wk[q] = __ldg(oc + c000 + off[q]) * t1 + __ldg(cc + c000 + off[q]) * t2;
+    float I = wk[0] * wgt[0][0] * wgt[0][1] * wgt[0][2];
+#pragma unroll
+    for (int q = 1; q < 8; q++) I = I + wk[q] * wgt[q][0] * wgt[q][1] * wgt[q][2];
+    float w = a.target[f][c];
+    // panels in the reference's order: bottom, top, front, back, left, right;
+    // the inner layer blends half and half, the outer layer takes I
+    auto apply = [&](int layer) {
+      const float frac = (float)(layer - 1) / 2.0f;
+      const float frac1 = 1.0f - frac;
+      w = frac * w + frac1 * I;
+    };
+    if (ks <= 2) apply(ks);
+    if (ks >= d.nz - 1) apply(d.nz - ks + 1);
+    if (js <= 2) apply(js);
+    if (js >= d.ny - 1) apply(d.ny - js + 1);
+    if (is <= 2) apply(is);
+    if (is >= d.nx - 1) apply(d.nx - is + 1);
+    a.target[f][c] = w;
+  }
 }
 
 // ------------------------------------------------------------ corer
@@ -347,7 +356,10 @@ void launch_bndry_inner(const InnerArgs& a, cudaStream_t s) {
 
 void launch_flanks(const FlanksArgs& a, cudaStream_t s) {
   const long n = shell_count(a.d, 2);
-  k_flanks<<<dim3((unsigned)((n + 255) / 256), (unsigned)a.nf), 256, 0, s>>>(a);
+  FlanksArgs b = a;
+  b.fields_per_block = 9;   // 34 fields in 4 launches-worth of blocks
+  const unsigned fy = (unsigned)((a.nf + b.fields_per_block - 1) / b.fields_per_block);
+  k_flanks<<<dim3((unsigned)((n + 255) / 256), fy), 256, 0, s>>>(b);
 }
 
 void launch_corer(const CorerArgs& a, cudaStream_t s) {

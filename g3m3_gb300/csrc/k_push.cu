@@ -236,7 +236,13 @@ __global__ void __launch_bounds__(256) k_push_field(const __grid_constant__ Push
 
 }  // namespace
 
-void launch_push_ion(const PushIonArgs& a, cudaStream_t s) {
+void launch_push_ion_tiled(const PushIonArgs& a, cudaStream_t s);
+
+void launch_push_ion(const PushIonArgs& a, cudaStream_t s) { launch_push_ion_tiled(a, s); }
+
+// The per-cell form (every neighbour through the L1 cache): the direct
+// statement of the stencil, kept for reference; the tiled kernel replaces it.
+void launch_push_ion_percell(const PushIonArgs& a, cudaStream_t s) {
   const dim3 blk(32, 4, 2);
   const dim3 grd = grid3(a.d, blk);
   if (is_pow2(2.0f * a.g.dx) && is_pow2(2.0f * a.g.dy) && is_pow2(2.0f * a.g.dz))

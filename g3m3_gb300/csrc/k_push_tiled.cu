@@ -1,0 +1,245 @@
+// k_push_tiled.cu -- push_ion (sub_push_ion.f90:4-362) staged through
+// shared memory.
+//
+// A block owns a TX x TY tile and marches along z.  For every plane it
+// stages the 13 fields that push_ion differentiates (the source state's
+// rho, px, py, pz and six pressures, and bs) together with the species
+// velocity v = p / max(rho, 1e-6) -- computed once per cell, as the
+// reference's pre-pass does (:67-81) -- in a 3-plane ring with a halo of
+// one cell.  The seven-point neighbours then come from shared memory and
+// the centre-only inputs (old state, btot, efld, tv) straight from HBM, so
+// each input is read from HBM about once.  The arithmetic is the per-cell
+// kernel's (k_push.cu), operation for operation.
+#include "kargs.cuh"
+#include "launch.cuh"
+
+namespace g3m3 {
+
+namespace {
+
+constexpr int TX = 32, TY = 8;
+constexpr int HX = TX + 2, HY = TY + 2;
+constexpr int NLOAD = 13;           // src 0..9, bs 0..2
+constexpr int NF = NLOAD + 3;       // + velocity x, y, z
+constexpr int VX = 13, VY = 14, VZ = 15;
+constexpr size_t SMEM = sizeof(float) * 3 * NF * HY * HX;
+
+__device__ __forceinline__ float& S(float* sm, int slot, int f, int ly, int lx) {
+  return sm[((slot * NF + f) * HY + ly) * HX + lx];
+}
+
+template <bool POW2>
+__global__ void __launch_bounds__(TX* TY, 3) k_push_ion_tiled(const __grid_constant__ PushIonArgs a, int kchunk) {
+  extern __shared__ float sm[];
+  const Dims d = a.d;
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+  const int i0 = blockIdx.x * TX + 1, j0 = blockIdx.y * TY + 1;
+  const int gi = i0 + tx, gj = j0 + ty;
+  const bool mine = gi <= nx && gj <= ny;
+  const bool inner_col = gi >= 2 && gi <= nx - 1 && gj >= 2 && gj <= ny - 1;
+  const size_t plane = (size_t)nx * ny;
+
+  const float* src[NLOAD];
+#pragma unroll
+  for (int f = 0; f < 10; f++) src[f] = a.src[f];
+  src[10] = a.bs[0]; src[11] = a.bs[1]; src[12] = a.bs[2];
+
+  auto load_plane = [&](int kp) {
+    const int slot = kp % 3;
+    for (int t = tid; t < HX * HY; t += TX * TY) {
+      const int ly = t / HX, lx = t % HX;
+      const int i = i0 - 1 + lx, j = j0 - 1 + ly;
+      float v[NLOAD];
+      if (kp >= 1 && kp <= nz && i >= 1 && i <= nx && j >= 1 && j <= ny) {
+        const size_t c = (size_t)(kp - 1) * plane + (size_t)(j - 1) * nx + (i - 1);
+#pragma unroll
+        for (int f = 0; f < NLOAD; f++) v[f] = __ldg(src[f] + c);
+        const float r = amax1(v[0], 1.e-6f);
+        S(sm, slot, VX, ly, lx) = v[1] / r;
+        S(sm, slot, VY, ly, lx) = v[2] / r;
+        S(sm, slot, VZ, ly, lx) = v[3] / r;
+      } else {
+#pragma unroll
+        for (int f = 0; f < NLOAD; f++) v[f] = 0.0f;
+        S(sm, slot, VX, ly, lx) = 0.0f;
+        S(sm, slot, VY, ly, lx) = 0.0f;
+        S(sm, slot, VZ, ly, lx) = 0.0f;
+      }
+#pragma unroll
+      for (int f = 0; f < NLOAD; f++) S(sm, slot, f, ly, lx) = v[f];
+    }
+  };
+
+  auto copy_old = [&](int k) {   // boundary cells of cur take the start-of-step state
+    if (!a.boundary_from_old || !mine) return;
+    const size_t c = (size_t)(k - 1) * plane + (size_t)(gj - 1) * nx + (gi - 1);
+#pragma unroll
+    for (int f = 0; f < 10; f++) a.out[f][c] = __ldg(a.old[f] + c);
+  };
+
+  // this block's planes: [k_lo, k_hi] of the interior 2..nz-1
+  const int k_lo = 2 + (int)blockIdx.z * kchunk;
+  const int k_hi = min(nz - 1, k_lo + kchunk - 1);
+  if (k_lo > k_hi) return;
+  if (blockIdx.z == 0) copy_old(1);
+  if (k_hi == nz - 1) copy_old(nz);
+  load_plane(k_lo - 1);
+  load_plane(k_lo);
+  const float delt = a.delt.get();
+  const float dxt = 2.0f * a.g.dx, dyt = 2.0f * a.g.dy, dzt = 2.0f * a.g.dz;
+  const float rdx = 1.0f / dxt, rdy = 1.0f / dyt, rdz = 1.0f / dzt;
+  const float bmax = 0.20f * a.rmass / delt / a.reynolds;
+  const float rey = a.reynolds;
+#define DV(a_, d_, rd_) dvd<POW2>((a_), (d_), (rd_))
+  for (int k = k_lo; k <= k_hi; k++) {
+    load_plane(k + 1);
+    __syncthreads();
+    if (mine && !inner_col) {
+      copy_old(k);
+    } else if (inner_col) {
+      const int sm1 = (k - 1) % 3, s0 = k % 3, sp1 = (k + 1) % 3;
+      const int ly = ty + 1, lx = tx + 1;
+      // field f at the centre and the six neighbours
+      auto C0 = [&](int f) { return S(sm, s0, f, ly, lx); };
+      auto XP = [&](int f) { return S(sm, s0, f, ly, lx + 1); };
+      auto XM = [&](int f) { return S(sm, s0, f, ly, lx - 1); };
+      auto YP = [&](int f) { return S(sm, s0, f, ly + 1, lx); };
+      auto YM = [&](int f) { return S(sm, s0, f, ly - 1, lx); };
+      auto ZP = [&](int f) { return S(sm, sp1, f, ly, lx); };
+      auto ZM = [&](int f) { return S(sm, sm1, f, ly, lx); };
+      auto fluxdiv = [&](int f) -> float {
+        return (DV(XP(f) * XP(VX) - XM(f) * XM(VX), dxt, rdx) + DV(YP(f) * YP(VY) - YM(f) * YM(VY), dyt, rdy))
+               + DV(ZP(f) * ZP(VZ) - ZM(f) * ZM(VZ), dzt, rdz);
+      };
+      const size_t c = (size_t)(k - 1) * plane + (size_t)(gj - 1) * nx + (gi - 1);
+      // centre-only inputs
+      const float old0 = __ldg(a.old[0] + c), old1 = __ldg(a.old[1] + c), old2 = __ldg(a.old[2] + c);
+      const float old3 = __ldg(a.old[3] + c), old4 = __ldg(a.old[4] + c), old5 = __ldg(a.old[5] + c);
+      const float old6 = __ldg(a.old[6] + c), old7 = __ldg(a.old[7] + c), old8 = __ldg(a.old[8] + c);
+      const float old9 = __ldg(a.old[9] + c);
+      const float bt = __ldg(a.btot + c);
+      const float e0 = __ldg(a.efld[0] + c), e1 = __ldg(a.efld[1] + c), e2 = __ldg(a.efld[2] + c);
+      const float tvx = __ldg(a.tv[0] + c), tvy = __ldg(a.tv[1] + c), tvz = __ldg(a.tv[2] + c);
+
+      const float o_rho = old0 - delt * ((DV(XP(1) - XM(1), dxt, rdx) + DV(YP(2) - YM(2), dyt, rdy))
+                                         + DV(ZP(3) - ZM(3), dzt, rdz));
+      const float aqpx = old1 - delt * fluxdiv(1);
+      const float aqpy = old2 - delt * fluxdiv(2);
+      const float aqpz = old3 - delt * fluxdiv(3);
+      float abx = C0(10), aby = C0(11), abz = C0(12);
+      float bmag = bt;
+      const float weight = amax1(1.0f, bmag / bmax);
+      const float skin_depth = rey / weight;
+      const float tcx = (tvy * abz - tvz * aby);
+      const float tcy = -(tvx * abz - tvz * abx);
+      const float tcz = (tvx * aby - tvy * abx);
+      const float v0x = C0(VX), v0y = C0(VY), v0z = C0(VZ);
+      const float qcx = (v0y * abz - v0z * aby);
+      const float qcy = -(v0x * abz - v0z * abx);
+      const float qcz = (v0x * aby - v0y * abx);
+      const float gpx = DV(XP(4) - XM(4), dxt, rdx) + DV(YP(7) - YM(7), dxt, rdx) + DV(ZP(8) - ZM(8), dxt, rdx);
+      const float gpy = DV(XP(7) - XM(7), dxt, rdx) + DV(YP(5) - YM(5), dyt, rdy) + DV(ZP(9) - ZM(9), dxt, rdx);
+      const float gpz = DV(XP(8) - XM(8), dxt, rdx) + DV(YP(9) - YM(9), dyt, rdy) + DV(ZP(6) - ZM(6), dzt, rdz);
+      const float dex = (e0 + tcx) * rey;
+      const float dey = (e1 + tcy) * rey;
+      const float dez = (e2 + tcz) * rey;
+      const float dvx = (qcx - tcx) * skin_depth;
+      const float dvy = (qcy - tcy) * skin_depth;
+      const float dvz = (qcz - tcz) * skin_depth;
+      const float rho_c = C0(0);
+      const float qden = rho_c / a.rmass;
+      const float npx = aqpx + delt * (qden * (dex + dvx) - gpx);
+      const float npy = aqpy + delt * (qden * (dey + dvy) - gpy);
+      const float npz = aqpz + delt * (qden * (dez + dvz) - gpz);
+      const float ax = a.g.xmin + a.g.dx * (float)(gi - 1);
+      const float ay = a.g.ymin + a.g.dy * (float)(gj - 1);
+      const float az = a.g.zmin + a.g.dz * (float)(k - 1);
+      const float radius = sqrtf(ax * ax + ay * ay + az * az) + 0.0000001f;
+      const float rr = a.re_equiv * radius;
+      const float g = delt * rho_c * a.grav / (rr * rr);
+      const float o_px = npx - g * ax / radius;
+      const float o_py = npy - g * ay / radius;
+      const float o_pz = npz - g * az / radius;
+
+      const float wx = C0(4), wy = C0(5), wz = C0(6), wxy = C0(7), wxz = C0(8), wyz = C0(9);
+      const float t2 = 2.0f * delt;
+      const float px_ = old4 - delt * fluxdiv(4) - DV(t2 * wx * (XP(VX) - XM(VX)), dxt, rdx);
+      const float py_ = old5 - delt * fluxdiv(5) - DV(t2 * wy * (YP(VY) - YM(VY)), dyt, rdy);
+      const float pz_ = old6 - delt * fluxdiv(6) - DV(t2 * wz * (ZP(VZ) - ZM(VZ)), dzt, rdz);
+      abx = (6.0f * abx + XP(10) + XM(10) + YP(10) + YM(10) + ZP(10) + ZM(10)) / 12.0f;
+      aby = (6.0f * aby + XP(11) + XM(11) + YP(11) + YM(11) + ZP(11) + ZM(11)) / 12.0f;
+      abz = (6.0f * abz + XP(12) + XM(12) + YP(12) + YM(12) + ZP(12) + ZM(12)) / 12.0f;
+      bmag = sqrtf(abx * abx + aby * aby + abz * abz);
+      float skin = rey;
+      if (bmag > bmax) skin = rey * (bmax / bmag);
+      const float gy2 = t2 * skin / a.rmass;
+      const float o_xx = px_ - DV(t2 * wxy * (YP(VX) - YM(VX)), dyt, rdy) - DV(t2 * wxz * (ZP(VX) - ZM(VX)), dzt, rdz)
+                         + gy2 * (wxy * abz - wxz * aby);
+      const float o_yy = py_ - DV(t2 * wxy * (XP(VY) - XM(VY)), dxt, rdx) - DV(t2 * wyz * (ZP(VY) - ZM(VY)), dzt, rdz)
+                         + gy2 * (wyz * abx - wxy * abz);
+      const float o_zz = pz_ - DV(t2 * wxz * (XP(VZ) - XM(VZ)), dxt, rdx) - DV(t2 * wyz * (YP(VZ) - YM(VZ)), dyt, rdy)
+                         + gy2 * (wxz * aby - wyz * abx);
+      const float gy1 = delt * skin / a.rmass;
+      const float o_xy = old7 - delt * fluxdiv(7)
+                         - delt * wxy * (DV(XP(VX) - XM(VX), dxt, rdx) + DV(YP(VY) - YM(VY), dyt, rdy))
+                         - DV(delt * wy * (YP(VX) - YM(VX)), dyt, rdy)
+                         - DV(delt * wx * (XP(VY) - XM(VY)), dxt, rdx)
+                         - DV(delt * wyz * (ZP(VX) - ZM(VX)), dzt, rdz)
+                         - DV(delt * wxz * (ZP(VY) - ZM(VY)), dzt, rdz)
+                         + gy1 * (abz * (wy - wx) - aby * wyz + abx * wxz);
+      const float o_xz = old8 - delt * fluxdiv(8)
+                         - delt * wxz * (DV(XP(VX) - XM(VX), dxt, rdx) + DV(ZP(VZ) - ZM(VZ), dzt, rdz))
+                         - DV(delt * wz * (ZP(VX) - ZM(VX)), dzt, rdz)
+                         - DV(delt * wx * (XP(VZ) - XM(VZ)), dxt, rdx)
+                         - DV(delt * wyz * (YP(VX) - YM(VX)), dyt, rdy)
+                         - DV(delt * wxy * (YP(VZ) - YM(VZ)), dyt, rdy)
+                         + gy1 * (aby * (wx - wz) - abx * wxy + abz * wyz);
+      const float o_yz = old9 - delt * fluxdiv(9)
+                         - delt * wyz * (DV(YP(VY) - YM(VY), dyt, rdy) + DV(ZP(VZ) - ZM(VZ), dzt, rdz))
+                         - DV(delt * wy * (YP(VZ) - YM(VZ)), dyt, rdy)
+                         - DV(delt * wz * (ZP(VY) - ZM(VY)), dzt, rdz)
+                         - DV(delt * wxy * (XP(VZ) - XM(VZ)), dxt, rdx)
+                         - DV(delt * wxz * (XP(VY) - XM(VY)), dxt, rdx)
+                         + gy1 * (abx * (wz - wy) - abz * wxz + aby * wxy);
+      a.out[0][c] = o_rho; a.out[1][c] = o_px; a.out[2][c] = o_py; a.out[3][c] = o_pz;
+      a.out[4][c] = o_xx; a.out[5][c] = o_yy; a.out[6][c] = o_zz;
+      a.out[7][c] = o_xy; a.out[8][c] = o_xz; a.out[9][c] = o_yz;
+    }
+    __syncthreads();
+  }
+#undef DV
+}
+
+template <bool POW2>
+void set_smem() {
+  static bool done = false;
+  if (!done) {
+    cudaFuncSetAttribute(k_push_ion_tiled<POW2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
+    done = true;
+  }
+}
+
+}  // namespace
+
+void launch_push_ion_tiled(const PushIonArgs& a, cudaStream_t s) {
+  const dim3 blk(TX, TY, 1);
+  const int tiles = ((a.d.nx + TX - 1) / TX) * ((a.d.ny + TY - 1) / TY);
+  const int interior = a.d.nz - 2;
+  // about one resident wave: 152 SMs x 3 blocks (65 KB of shared memory each)
+  int chunks = (456 + tiles - 1) / tiles;
+  if (chunks > interior) chunks = interior;
+  if (chunks < 1) chunks = 1;
+  const int kchunk = (interior + chunks - 1) / chunks;
+  chunks = (interior + kchunk - 1) / kchunk;
+  const dim3 grd((unsigned)((a.d.nx + TX - 1) / TX), (unsigned)((a.d.ny + TY - 1) / TY), (unsigned)chunks);
+  if (is_pow2(2.0f * a.g.dx) && is_pow2(2.0f * a.g.dy) && is_pow2(2.0f * a.g.dz)) {
+    set_smem<true>();
+    k_push_ion_tiled<true><<<grd, blk, SMEM, s>>>(a, kchunk);
+  } else {
+    set_smem<false>();
+    k_push_ion_tiled<false><<<grd, blk, SMEM, s>>>(a, kchunk);
+  }
+}
+
+}  // namespace g3m3
