@@ -280,6 +280,31 @@ int g3m3_divb_correct(g3m3_ctx* ctx, int nx, int ny, int nz, int n_grids,
     int box, int nbands, const int* divb_band_pos, const float* xspac,
     float divb_errlim, float* bx, float* by, float* bz, int* iters);
 
+/* ---- g3m3_divb_correct without device allocation (no counterpart in the
+ * reference) ------------------------------------------------------------
+ * Same arguments, arithmetic and results as g3m3_divb_correct, for callers
+ * that must not allocate device memory once they run: a host code that
+ * gives the whole device to its own memory pool at start-up, or one that
+ * keeps other streams busy and cannot take the device-wide synchronisation
+ * cudaMalloc and cudaFree may bring.  g3m3_divb_correct grows scratch with
+ * cudaMalloc and copies host arrays into new device buffers; this call does
+ * neither.  The solver's state and vectors live in one fixed array inside
+ * the library (28 MiB per device), which holds boxes of up to
+ * G3M3_NOALLOC_DIVB_MAX_CELLS cells; larger boxes are rejected with
+ * G3M3_ERR_ARG.  bx, by, bz must be device (or managed) memory, else
+ * G3M3_ERR_ARG; xspac and divb_band_pos may be host or device arrays.
+ * The first call on each device finds the array's address there (which may
+ * load the library's device code holding it): make that first call before
+ * any stream capture.  Every call on a device shares the one array, which
+ * keeps the last call's contents (each call resets what the solver needs
+ * zeroed); calls that overlap in time, from two threads or on two streams,
+ * race on it and must be serialised by the caller. */
+#define G3M3_NOALLOC_DIVB_MAX_CELLS 1048576
+int g3m3_divb_correct_noalloc(g3m3_ctx* ctx, int nx, int ny, int nz,
+    int n_grids, int box, int nbands, const int* divb_band_pos,
+    const float* xspac, float divb_errlim, float* bx, float* by, float* bz,
+    int* iters);
+
 /* ---- a19: virtual spacecraft -- findgrid cft_findgrid.f90:4 and
  * trilin_interp cft_trilin_interp.f90:10, batched over n trajectory points:
  * xyz(3,n) in planet radii; out(n) = trilinear value of field at each point
