@@ -41,6 +41,22 @@ def dist_env():
     return ws, rank, local
 
 
+def replica_reduce(max_vals, sum_vals):
+    """Whole-job figures of N independent replicas (one per rank): the
+    slowest rank's times (max) and the work of all ranks (sum).  Without an
+    initialised process group the values are returned unchanged."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [float(x) for x in max_vals], [float(x) for x in sum_vals]
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x) for x in max_vals], dtype=torch.float64, device=dev)
+    u = torch.tensor([float(x) for x in sum_vals], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return [float(x) for x in t.tolist()], [float(x) for x in u.tolist()]
+
+
 class Clocks:
     """nvidia-smi samples while the timed region runs."""
 
@@ -169,28 +185,24 @@ def run_ours(args):
     # this overwrites the wrk/old copies, so it runs after the timed legs
     rows = kernel_table(m)
     roof = roofline_from(rows)
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms_g, ms_p, e2e_s], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_g, ms_p, e2e_s = (float(x) for x in t.tolist())
+    (ms_g, ms_p, e2e_s), (cu_g, cu_p, cu_e, k_g) = replica_reduce([ms_g, ms_p, e2e_s], [cu_g, cu_p, cu_e, k_g])
     m.close()
     ctx.close()
     if rank != 0:
         return None
-    value = ws * cu_g / (ms_g / 1e3)
+    value = cu_g / (ms_g / 1e3)
     line = {
         "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_g / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded state from the "
         "reference's initial-condition formulas + 1% noise)",
         "config": {"workload": WORKLOAD, "boxes": p.n_grids, "box": [p.nx, p.ny, p.nz],
-                   "cells_per_box": p.nx * p.ny * p.nz, "cell_updates_per_step": cu_g / args.steps,
+                   "cells_per_box": p.nx * p.ny * p.nz, "cell_updates_per_step": cu_g / args.steps / ws,
                    "mode": "one CUDA graph per main step", "l2": "working set (>400 MB per box) exceeds L2",
                    "parallelism": f"replicas x{ws}"},
-        "plain": {"value": ws * cu_p / (ms_p / 1e3), "ms_per_step": ms_p / max(2, args.steps // 2),
+        "plain": {"value": cu_p / (ms_p / 1e3), "ms_per_step": ms_p / max(2, args.steps // 2),
                   "mode": "kernels launched from the host loop"},
-        "e2e": {"value": ws * cu_e / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": 34 * n4 * 4,
+        "e2e": {"value": cu_e / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": 34 * n4 * 4,
                 "d2h_bytes_per_step": 34 * n4 * 4,
                 "path": "g3m3_model_set_state (pinned host) + g3m3_model_run(1 step) + g3m3_model_get_state"},
         "gpu_launches": int(k_g),
@@ -198,7 +210,7 @@ def run_ours(args):
         "kernels": rows,
         "clocks": clk,
     }
-    if not args.no_cpu:
+    if not args.no_cpu and ws == 1:
         line["cpu_baseline"] = cpu_baseline()
     return line
 
