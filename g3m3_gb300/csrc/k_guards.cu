@@ -17,6 +17,8 @@
 // Both routines therefore run as one pass over the box plus a scatter of
 // the (rare) flagged cells.  Max-speed reductions are warp-shuffle maxima
 // folded into 5 device words with atomicMax on the (non-negative) float bits.
+#include <cooperative_groups.h>
+
 #include "kargs.cuh"
 #include "launch.cuh"
 
@@ -62,9 +64,13 @@ __device__ __forceinline__ bool floor_sp(Sp& v, float rmin) {
   return false;
 }
 
-// deferred store of a species' ten values at cell c
+// deferred store of a species' ten values at cell c; the threads of a warp
+// that append together take consecutive slots with one counter update
 __device__ __forceinline__ void append(const GuardArgs& a, size_t c, int s, const Sp& v) {
-  const unsigned slot = atomicAdd(a.list_count, 1u);
+  const cooperative_groups::coalesced_group g = cooperative_groups::coalesced_threads();
+  unsigned base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(a.list_count, g.size());
+  const unsigned slot = g.shfl(base, 0) + g.thread_rank();
   if (slot >= a.list_cap) return;   // counted: the host reports the overflow
   float* e = a.list + (size_t)slot * 11;
   e[0] = __uint_as_float((unsigned)(c * 4 + (size_t)s));
@@ -113,7 +119,6 @@ __global__ void __launch_bounds__(256) k_guards(const __grid_constant__ GuardArg
         a.f[b + 0][c] = v.r;
         a.f[b + 4][c] = v.xx; a.f[b + 5][c] = v.yy; a.f[b + 6][c] = v.zz;
         a.f[b + 7][c] = 0.0f; a.f[b + 8][c] = 0.0f; a.f[b + 9][c] = 0.0f;
-        a.f[b + 7][c] = v.xy; a.f[b + 8][c] = v.xz; a.f[b + 9][c] = v.yz;
         continue;
       }
       if (!(a.do_speed && interior)) {
@@ -184,14 +189,20 @@ __global__ void __launch_bounds__(256) k_guards(const __grid_constant__ GuardArg
     if (ep_changed) a.f[G3M3_F_EPRES][c] = ep;
   }
   if (a.do_speed) {
+    // warp maxima, then block maxima, then one atomic per block and word
+    __shared__ float wmax[5][8];
     mx = warp_max(mx); my = warp_max(my); mz = warp_max(mz); mc = warp_max(mc); ma = warp_max(ma);
-    const int lane = (threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z)) & 31;
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int lane = tid & 31, warp = tid >> 5;
     if (lane == 0) {
-      if (mx > 0.0f) atomicMax(a.maxbits + 0, __float_as_uint(mx));
-      if (my > 0.0f) atomicMax(a.maxbits + 1, __float_as_uint(my));
-      if (mz > 0.0f) atomicMax(a.maxbits + 2, __float_as_uint(mz));
-      if (mc > 0.0f) atomicMax(a.maxbits + 3, __float_as_uint(mc));
-      if (ma > 0.0f) atomicMax(a.maxbits + 4, __float_as_uint(ma));
+      wmax[0][warp] = mx; wmax[1][warp] = my; wmax[2][warp] = mz; wmax[3][warp] = mc; wmax[4][warp] = ma;
+    }
+    __syncthreads();
+    if (tid < 5) {
+      float m = wmax[tid][0];
+#pragma unroll
+      for (int w = 1; w < 8; w++) m = amax1(m, wmax[tid][w]);
+      if (m > 0.0f) atomicMax(a.maxbits + tid, __float_as_uint(m));
     }
   }
 }
