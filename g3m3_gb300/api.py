@@ -151,6 +151,16 @@ class Model:
             addr(li["ijzero"]), addr(li["numzero"]), addr(li["parm_zero"]), li["ijzero"].shape[0]))
         self.ctx.synchronize()
 
+    def set_variant(self, kernel: int, variant: int):
+        self.ctx.check(self.L.g3m3_model_set_variant(self.h, kernel, variant))
+
+    def autotune(self):
+        """Times the tile-shape variants on this model's box size and keeps
+        the fastest; returns the chosen fcsmooth variant."""
+        v = ctypes.c_int(-1)
+        self.ctx.check(self.L.g3m3_model_autotune(self.h, ctypes.byref(v)))
+        return v.value
+
     def init_steps(self):
         self.ctx.check(self.L.g3m3_model_init_steps(self.h))
 

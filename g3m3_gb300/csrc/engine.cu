@@ -69,6 +69,7 @@ struct g3m3_model {
   int nsteps_done = 0;
   float iso_flag = 1.0f;
   int64_t kernels = 0, graph_launches = 0;
+  int fcs_variant = 0;               // fcsmooth tile shape (g3m3_model_autotune)
   std::map<std::string, cudaGraphExec_t> graphs;
   std::map<std::string, int64_t> kernel_nodes;
   int64_t launches_in_step = 0;
@@ -481,7 +482,7 @@ int enqueue_box_step(g3m3_model* m, const Action& act) {
     fa.wrk[q] = W(m, q, b);
     fa.chi[q] = q >= G3M3_F_BX ? p.diferg : p.difrho;
   }
-  fa.nf = G3M3_NFIELDS; fa.d = m->d;
+  fa.nf = G3M3_NFIELDS; fa.d = m->d; fa.variant = m->fcs_variant;
   launch_fcsmooth(fa, S(m));
   m->launches_in_step += 1;
   boundary_stage(m, C, b, act.s_t1c);
@@ -877,7 +878,7 @@ int g3m3_model_time_kernel(g3m3_model* m, int kernel, int box, int reps, float* 
           fa.px[q] = O(m, q, b); fa.old[q] = C(m, q, b); fa.wrk[q] = W(m, q, b);
           fa.chi[q] = q >= G3M3_F_BX ? p.diferg : p.difrho;
         }
-        fa.nf = G3M3_NFIELDS; fa.d = m->d;
+        fa.nf = G3M3_NFIELDS; fa.d = m->d; fa.variant = m->fcs_variant;
         launch_fcsmooth(fa, s);
         by = 12.0 * G3M3_NFIELDS * n3;   // wrk, old read, result written, per field
         return 0;
@@ -949,6 +950,62 @@ int g3m3_model_time_kernel(g3m3_model* m, int kernel, int box, int reps, float* 
   *ms_per_launch = ms / (float)reps;
   if (bytes) *bytes = by;
   return G3M3_OK;
+}
+
+int g3m3_model_set_variant(g3m3_model* m, int kernel, int variant) {
+  if (!m || kernel != 1 || variant < 0 || variant > 1) return G3M3_ERR_ARG;
+  if (m->fcs_variant != variant) {
+    // captured graphs hold the old launch shape
+    for (auto& kv : m->graphs) cudaGraphExecDestroy(kv.second);
+    m->graphs.clear();
+    m->kernel_nodes.clear();
+    m->fcs_variant = variant;
+  }
+  return G3M3_OK;
+}
+
+int g3m3_model_autotune(g3m3_model* m, int* fcs_variant) {
+  if (!m) return G3M3_ERR_ARG;
+  cudaStream_t s = m->ctx->stream;
+  const size_t n3 = m->n3;
+  // scratch copies of box 1's current, old and wrk fields: timing runs on
+  // realistic values without touching the state
+  float* tmp = nullptr;
+  G3M3_CUDA(m->ctx, cudaMalloc(&tmp, 3 * (size_t)G3M3_NFIELDS * n3 * sizeof(float)));
+  FcsArgs fa{};
+  cudaError_t e = cudaSuccess;
+  for (int q = 0; q < G3M3_NFIELDS && e == cudaSuccess; q++) {
+    float* px = tmp + (size_t)q * n3;
+    float* od = tmp + (size_t)(G3M3_NFIELDS + q) * n3;
+    float* wk = tmp + (size_t)(2 * G3M3_NFIELDS + q) * n3;
+    e = cudaMemcpyAsync(od, O(m, q, 1), n3 * sizeof(float), cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(wk, C(m, q, 1), n3 * sizeof(float), cudaMemcpyDeviceToDevice, s);
+    fa.px[q] = px; fa.old[q] = od; fa.wrk[q] = wk;
+    fa.chi[q] = q >= G3M3_F_BX ? m->p.diferg : m->p.difrho;
+  }
+  fa.nf = G3M3_NFIELDS; fa.d = m->d;
+  float best_ms = 0.0f;
+  int best = 0;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  for (int v = 0; v <= 1 && e == cudaSuccess; v++) {
+    fa.variant = v;
+    launch_fcsmooth(fa, s);   // warm-up
+    cudaEventRecord(e0, s);
+    for (int r = 0; r < 5; r++) launch_fcsmooth(fa, s);
+    cudaEventRecord(e1, s);
+    e = cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e == cudaSuccess && (v == 0 || ms < best_ms)) { best_ms = ms; best = v; }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(tmp);
+  if (e != cudaSuccess) return cuda_check(m->ctx, e, "autotune");
+  if (fcs_variant) *fcs_variant = best;
+  return g3m3_model_set_variant(m, 1, best);
 }
 
 int g3m3_model_times(g3m3_model* m, double* t, double* t_stepnew, int64_t* cell_updates) {

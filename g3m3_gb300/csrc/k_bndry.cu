@@ -250,30 +250,48 @@ __global__ void __launch_bounds__(256) k_flanks(const __grid_constant__ FlanksAr
   const size_t c = d.at(is, js, ks);
   const int f_lo = blockIdx.y * a.fields_per_block;
   const int f_hi = min(a.nf, f_lo + a.fields_per_block);
-  for (int f = f_lo; f < f_hi; f++) {
-    const float* __restrict__ oc = a.oldc[f];
-    const float* __restrict__ cc = a.curc[f];
-    float wk[8];
+  // fields in groups of G: every load of a group is issued before its
+  // stores, so the loads of a group overlap one another
+  constexpr int G = 3;
+  for (int f0 = f_lo; f0 < f_hi; f0 += G) {
+    float wo[G][8], wc[G][8], tw[G];
 #pragma unroll
-    for (int q = 0; q < 8; q++) wk[q] = __ldg(oc + c000 + off[q]) * t1 + __ldg(cc + c000 + off[q]) * t2;
-    float I = wk[0] * wgt[0][0] * wgt[0][1] * wgt[0][2];
+    for (int g = 0; g < G; g++) {
+      if (f0 + g >= f_hi) break;
+      const float* __restrict__ oc = a.oldc[f0 + g];
+      const float* __restrict__ cc = a.curc[f0 + g];
 #pragma unroll
-    for (int q = 1; q < 8; q++) I = I + wk[q] * wgt[q][0] * wgt[q][1] * wgt[q][2];
-    float w = a.target[f][c];
-    // panels in the reference's order: bottom, top, front, back, left, right;
-    // the inner layer blends half and half, the outer layer takes I
-    auto apply = [&](int layer) {
-      const float frac = (float)(layer - 1) / 2.0f;
-      const float frac1 = 1.0f - frac;
-      w = frac * w + frac1 * I;
-    };
-    if (ks <= 2) apply(ks);
-    if (ks >= d.nz - 1) apply(d.nz - ks + 1);
-    if (js <= 2) apply(js);
-    if (js >= d.ny - 1) apply(d.ny - js + 1);
-    if (is <= 2) apply(is);
-    if (is >= d.nx - 1) apply(d.nx - is + 1);
-    a.target[f][c] = w;
+      for (int q = 0; q < 8; q++) {
+        wo[g][q] = __ldg(oc + c000 + off[q]);
+        wc[g][q] = __ldg(cc + c000 + off[q]);
+      }
+      tw[g] = a.target[f0 + g][c];
+    }
+#pragma unroll
+    for (int g = 0; g < G; g++) {
+      if (f0 + g >= f_hi) break;
+      float wk[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) wk[q] = wo[g][q] * t1 + wc[g][q] * t2;
+      float I = wk[0] * wgt[0][0] * wgt[0][1] * wgt[0][2];
+#pragma unroll
+      for (int q = 1; q < 8; q++) I = I + wk[q] * wgt[q][0] * wgt[q][1] * wgt[q][2];
+      float w = tw[g];
+      // panels in the reference's order: bottom, top, front, back, left,
+      // right; the inner layer blends half and half, the outer layer takes I
+      auto apply = [&](int layer) {
+        const float frac = (float)(layer - 1) / 2.0f;
+        const float frac1 = 1.0f - frac;
+        w = frac * w + frac1 * I;
+      };
+      if (ks <= 2) apply(ks);
+      if (ks >= d.nz - 1) apply(d.nz - ks + 1);
+      if (js <= 2) apply(js);
+      if (js >= d.ny - 1) apply(d.ny - js + 1);
+      if (is <= 2) apply(is);
+      if (is >= d.nx - 1) apply(d.nx - is + 1);
+      a.target[f0 + g][c] = w;
+    }
   }
 }
 
@@ -357,7 +375,7 @@ void launch_bndry_inner(const InnerArgs& a, cudaStream_t s) {
 void launch_flanks(const FlanksArgs& a, cudaStream_t s) {
   const long n = shell_count(a.d, 2);
   FlanksArgs b = a;
-  b.fields_per_block = 9;   // 34 fields in 4 launches-worth of blocks
+  b.fields_per_block = 6;   // 34 fields over 6 rows of blocks
   const unsigned fy = (unsigned)((a.nf + b.fields_per_block - 1) / b.fields_per_block);
   k_flanks<<<dim3((unsigned)((n + 255) / 256), fy), 256, 0, s>>>(b);
 }

@@ -140,9 +140,9 @@ void launch_vtot(const VtotArgs& a, cudaStream_t s) {
   k_vtot<<<blocks_for(a.d.cells(), 256), 256, 0, s>>>(a);
 }
 
-void launch_fcsmooth_tiled(const FcsArgs& a, cudaStream_t s);
+void launch_fcsmooth_tiled(const FcsArgs& a, cudaStream_t s, int variant);
 
-void launch_fcsmooth(const FcsArgs& a, cudaStream_t s) { launch_fcsmooth_tiled(a, s); }
+void launch_fcsmooth(const FcsArgs& a, cudaStream_t s) { launch_fcsmooth_tiled(a, s, a.variant); }
 
 // One thread per cell re-deriving every intermediate: kept as the simple
 // statement of the algorithm (not launched by the library).

@@ -117,6 +117,7 @@ struct FcsArgs {           // fcsmooth for up to 34 fields
   float chi[G3M3_NFIELDS];
   int nf;
   Dims d;
+  int variant;              // tile shape (launch_fcsmooth); 0 = default
 };
 
 struct GuardArgs {         // set_rho and/or set_speed_agrd

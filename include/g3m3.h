@@ -342,6 +342,13 @@ int g3m3_model_run(g3m3_model* m, int nsteps, int use_graph);
 /* div B cleaning of every box plus flanks_synced and bndry_corer
  * (3d_main.f90:3363-3408). */
 int g3m3_model_divb_all(g3m3_model* m);
+/* Tile shapes.  kernel 1 = fcsmooth: variant 0 = 32x8 tiles, 1 = 32x16.
+ * Every variant gives the same bits; only the speed differs.
+ * g3m3_model_autotune times each variant on scratch copies of box 1 (the
+ * state is not changed), keeps the fastest and reports it; cached step
+ * graphs are dropped when the choice changes. */
+int g3m3_model_set_variant(g3m3_model* m, int kernel, int variant);
+int g3m3_model_autotune(g3m3_model* m, int* fcs_variant);
 /* Time bookkeeping: t, t_stepnew(1..n_grids), executed cell-updates. */
 int g3m3_model_times(g3m3_model* m, double* t, double* t_stepnew,
     int64_t* cell_updates);

@@ -12,7 +12,7 @@ from g3m3_gb300.state import make_config
 pytestmark = pytest.mark.gpu
 
 
-def run_pair(cfg, nsteps, graph=False, **over):
+def run_pair(cfg, nsteps, graph=False, variant=None, autotune=False, **over):
     from oracle.oracle import OracleModel
     from g3m3_gb300.api import Context, Model
     st = make_config(cfg, **over)
@@ -20,6 +20,10 @@ def run_pair(cfg, nsteps, graph=False, **over):
     om.init_steps()
     with Context() as ctx:
         m = Model(ctx, st)
+        if variant is not None:
+            m.set_variant(1, variant)
+        if autotune:
+            assert m.autotune() in (0, 1)
         m.init_steps()
         assert np.array_equal(m.times()[1], om.t_stepnew), (m.times()[1], om.t_stepnew)
         for _ in range(nsteps):
@@ -80,3 +84,21 @@ def test_divb_all():
         assert rel_l2(g[q] - st.cur[q], om.cur[q] - st.cur[q]) < 0.2
     for q in range(31):
         assert_same(g[q], om.cur[q], f"divb untouched field {q}")
+
+
+@pytest.mark.parametrize("cfg,nsteps", [("tiny3", 2), ("mid3", 2)])
+def test_fcsmooth_tall_tiles(cfg, nsteps):
+    """The 32x16-tile flux correction gives the same bits as the oracle."""
+    om, g, (t, tsn, cu, k, gl) = run_pair(cfg, nsteps, variant=1)
+    for q in range(34):
+        assert_same(g[q], om.cur[q], f"{cfg} field {q}")
+    assert np.array_equal(tsn, om.t_stepnew)
+
+
+def test_autotuned_steps():
+    """Autotuning picks a tile shape on scratch copies: the state it leaves
+    and the steps after it are the oracle's."""
+    om, g, (t, tsn, cu, k, gl) = run_pair("mid3", 2, graph=True, autotune=True)
+    for q in range(34):
+        assert_same(g[q], om.cur[q], f"mid3 field {q}")
+    assert np.array_equal(tsn, om.t_stepnew)
