@@ -255,6 +255,16 @@ def kernel_table(m, reps=20):
     return rows
 
 
+# DRAM bytes (read + write) per launch from one ncu capture of each kernel
+# on a 121x121x61 box (profiles/*_121x121x61.md)
+NCU_TRAFFIC = {
+    "fcsmooth x34": 243.07e6 + 96.28e6,
+    "push_ion": 73.79e6 + 6.69e6,
+    "set_rho+set_speed_agrd": 100.11e6 + 4.78e6,
+    "flanks x34": 82.79e6 + 4.61e6,
+}
+
+
 def roofline_from(rows):
     name = max(rows, key=lambda k: rows[k]["ms_per_launch"] * rows[k]["launches_per_box_step"])
     r = rows[name]
@@ -262,7 +272,9 @@ def roofline_from(rows):
     return {"kernel": name + " (121x121x61 box)", "bound": "hbm", "achieved": r["achieved_gbs"], "peak": peak,
             "unit": "GB/s", "frac": r["achieved_gbs"] / peak, "peak_source": kind,
             "ms_per_launch": r["ms_per_launch"], "algorithmic_bytes_per_launch": r["algorithmic_bytes_per_launch"],
-            "traffic": None}
+            "traffic": NCU_TRAFFIC.get(name),
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch" if name in NCU_TRAFFIC
+            else None}
 
 
 def cpu_baseline(max_seconds: float = 25.0):
