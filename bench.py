@@ -224,9 +224,59 @@ def run_ours(args):
         "kernels": rows,
         "clocks": clk,
     }
+    if not args.no_batched:
+        line["batched"] = run_batched(args, local)
     if not args.no_cpu and ws == 1:
         line["cpu_baseline"] = cpu_baseline()
     return line
+
+
+def run_batched(args, device, members=16):
+    """The upstream-condition ensemble: 16 nested grids (5 boxes each, box
+    sizes cycling 121x121x61, 97x97x49, 81x81x41; wind from the seed),
+    advanced with one CUDA graph per main step for all members, and plain
+    (members one after another, kernels launched from the host loop)."""
+    import torch
+    from g3m3_gb300.api import Context, Ensemble
+    from g3m3_gb300.state import ensemble_member
+    ctx = Context(device)
+    states = [ensemble_member(i) for i in range(members)]
+    ens = Ensemble(ctx, states)
+    cells = sorted({(st.params.nx, st.params.ny, st.params.nz) for st in states}, reverse=True)
+    del states
+    ens.init_steps()
+    stream = torch.cuda.ExternalStream(ens.stream)
+
+    def timed(nsteps, graph):
+        cu0 = ens.stats()[2]
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        ens.run(nsteps, graph=graph)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        k, _, cu1 = ens.stats()
+        return e0.elapsed_time(e1), cu1 - cu0, k
+
+    ens.run(max(args.warmup, 2), graph=True)   # captures the step graphs
+    ens.run(1, graph=False)
+    ms_g, cu_g, k_g = timed(args.steps, True)
+    n_p = max(2, args.steps // 2)
+    ms_p, cu_p, _ = timed(n_p, False)
+    ens.close()
+    ctx.close()
+    vg, vp = cu_g / (ms_g / 1e3), cu_p / (ms_p / 1e3)
+    return {"workload": f"ensemble of {members} nested grids, 5 boxes each, box sizes "
+                        + ", ".join(f"{a}x{b}x{c}" for a, b, c in cells) + " cycling; upstream n, |v|, IMF "
+                        "clock angle and |B| drawn from the seed",
+            "members": members,
+            "graph": {"value": vg, "unit": "cell-updates/s", "ms_per_step": ms_g / args.steps, "steps": args.steps,
+                      "gpu_launches": int(k_g), "mode": "one CUDA graph per main step for all members, "
+                      "members on their own streams"},
+            "plain": {"value": vp, "unit": "cell-updates/s", "ms_per_step": ms_p / n_p, "steps": n_p,
+                      "mode": "members one after another, kernels launched from the host loop"},
+            "graph_over_plain": vg / vp}
 
 
 KERNELS = {  # id: (name, launches per box-step)
@@ -350,6 +400,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 16-member ensemble leg")
     ap.add_argument("--profile", action="store_true",
                     help="profiling case for ncu: one 121x121x61 box, warmup+steps main steps, host-loop launches")
     args = ap.parse_args()

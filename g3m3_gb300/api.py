@@ -122,14 +122,21 @@ class Context:
 class Model:
     """A multi-box state on the device advanced by the step engine."""
 
-    def __init__(self, ctx: Context, state):
+    def __init__(self, ctx: Context, state, handle=None):
+        """A new model for ``state``; with ``handle``, a view of a model the
+        library already holds (an ensemble member), which this object loads
+        with ``state`` but does not destroy."""
         self.ctx = ctx
         self.L = ctx.L
         self.p = state.params
-        h = ctypes.c_void_p()
-        ctx.check(self.L.g3m3_model_create(ctx.h, ctypes.byref(self.p), ctypes.byref(h)))
-        self.h = h
-        ctx._models.append(self)
+        self.owned = handle is None
+        if handle is None:
+            h = ctypes.c_void_p()
+            ctx.check(self.L.g3m3_model_create(ctx.h, ctypes.byref(self.p), ctypes.byref(h)))
+            self.h = h
+            ctx._models.append(self)
+        else:
+            self.h = handle
         self.upload(state)
 
     def upload(self, state):
@@ -207,8 +214,57 @@ class Model:
         return self.L.g3m3_model_stream(self.h)
 
     def close(self):
-        if self.h and self.ctx.h:
+        if self.h and self.ctx.h and self.owned:
             self.L.g3m3_model_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Ensemble:
+    """Independent states (box sizes may differ) advanced together: with
+    ``graph=True`` one main step of every member is one CUDA graph, the
+    members' kernels overlapping on their own streams."""
+
+    def __init__(self, ctx: Context, states):
+        self.ctx = ctx
+        self.L = ctx.L
+        self._params = (G3M3Params * len(states))(*[st.params for st in states])
+        h = ctypes.c_void_p()
+        ctx.check(self.L.g3m3_ensemble_create(ctx.h, len(states), self._params, ctypes.byref(h)))
+        self.h = h
+        ctx._models.append(self)
+        self.members = []
+        for i, st in enumerate(states):
+            mh = ctypes.c_void_p()
+            ctx.check(self.L.g3m3_ensemble_member(h, i, ctypes.byref(mh)))
+            self.members.append(Model(ctx, st, handle=mh))
+
+    def init_steps(self):
+        for m in self.members:
+            m.init_steps()
+
+    def run(self, nsteps: int, graph: bool = True):
+        self.ctx.check(self.L.g3m3_ensemble_run(self.h, nsteps, 1 if graph else 0))
+
+    def stats(self):
+        k, g, cu = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        self.ctx.check(self.L.g3m3_ensemble_stats(self.h, ctypes.byref(k), ctypes.byref(g), ctypes.byref(cu)))
+        return k.value, g.value, cu.value
+
+    @property
+    def stream(self):
+        return self.L.g3m3_ensemble_stream(self.h)
+
+    def close(self):
+        if self.h and self.ctx.h:
+            for m in self.members:
+                m.h = None
+            self.L.g3m3_ensemble_destroy(self.h)
         self.h = None
 
     def __del__(self):

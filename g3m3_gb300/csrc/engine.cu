@@ -36,6 +36,8 @@ using namespace g3m3;
 
 struct g3m3_model {
   g3m3_ctx* ctx = nullptr;
+  cudaStream_t stream = nullptr;     // the context's stream, or the member's own in an ensemble
+  bool own_stream = false;
   g3m3_params p{};
   Dims d{};
   size_t n3 = 0, n4 = 0;
@@ -92,7 +94,7 @@ int scal_slot(g3m3_model* m, float v) {
 
 ScalarRef sref(g3m3_model* m, int slot) { return ScalarRef{m->h_scal[slot], m->d_scal + slot}; }
 
-cudaStream_t S(g3m3_model* m) { return m->ctx->stream; }
+cudaStream_t S(g3m3_model* m) { return m->stream; }
 
 void fields_stage(g3m3_model* m, Getter src, int b) {
   const float rx = m->p.xspac[b - 1];
@@ -524,7 +526,7 @@ int alloc_model(g3m3_model* m) {
   size_t total = 3 * G3M3_NFIELDS * n4 + 3 * n4 + 2 * (size_t)mb * n3 + 19 * n3 + 7 * n3;
   cudaError_t e = cudaMalloc(&m->mem, total * sizeof(float));
   if (e != cudaSuccess) return cuda_check(m->ctx, e, "cudaMalloc(model)");
-  e = cudaMemsetAsync(m->mem, 0, total * sizeof(float), m->ctx->stream);
+  e = cudaMemsetAsync(m->mem, 0, total * sizeof(float), S(m));
   if (e != cudaSuccess) return cuda_check(m->ctx, e, "memset(model)");
   float* q = m->mem;
   for (int r = 0; r < 3; r++)
@@ -543,7 +545,7 @@ int alloc_model(g3m3_model* m) {
   if (e != cudaSuccess) return cuda_check(m->ctx, e, "cudaMalloc(limiter list)");
   const size_t nwords = 8 + 5 * (size_t)G3M3_MAX_GRIDS;
   if ((e = cudaMalloc(&m->words, nwords * sizeof(unsigned))) != cudaSuccess) return cuda_check(m->ctx, e, "words");
-  if ((e = cudaMemsetAsync(m->words, 0, nwords * sizeof(unsigned), m->ctx->stream)) != cudaSuccess)
+  if ((e = cudaMemsetAsync(m->words, 0, nwords * sizeof(unsigned), S(m))) != cudaSuccess)
     return cuda_check(m->ctx, e, "words");
   if ((e = cudaMallocHost(&m->host_words, nwords * sizeof(unsigned))) != cudaSuccess)
     return cuda_check(m->ctx, e, "host words");
@@ -557,8 +559,63 @@ int alloc_model(g3m3_model* m) {
   return G3M3_OK;
 }
 
+struct Roles { int cur[G3M3_MAX_GRIDS], old[G3M3_MAX_GRIDS]; };
+
+Roles save_roles(const g3m3_model* m) {
+  Roles r;
+  std::memcpy(r.cur, m->role_cur, sizeof r.cur);
+  std::memcpy(r.old, m->role_old, sizeof r.old);
+  return r;
+}
+
+void restore_roles(g3m3_model* m, const Roles& r) {
+  std::memcpy(m->role_cur, r.cur, sizeof r.cur);
+  std::memcpy(m->role_old, r.old, sizeof r.old);
+}
+
+// Host part of a main step: the schedule and scalar table, and the key of
+// the step's launch sequence (buffer roles + actions).
+int step_plan(g3m3_model* m, std::vector<Action>& acts, std::string& key) {
+  const std::string roles = plan_key(m, {});
+  int rc = plan_main_step(m, acts);
+  if (rc) return rc;
+  key = roles + plan_key(m, acts).substr(m->p.n_grids + 1);
+  return G3M3_OK;
+}
+
+// Device part of a main step on the model's stream: scalar upload, the
+// kernels, the read-back of the recorded maxima.  Advances the buffer roles.
+int step_enqueue(g3m3_model* m, const std::vector<Action>& acts) {
+  const size_t nwords = 8 + 5 * (size_t)G3M3_MAX_GRIDS;
+  cudaError_t e;
+  m->launches_in_step = 0;
+  if ((e = cudaMemcpyAsync(m->d_scal, m->h_scal, m->scal_cap * sizeof(float), cudaMemcpyHostToDevice, S(m))) !=
+      cudaSuccess)
+    return cuda_check(m->ctx, e, "scalar upload");
+  int rc = enqueue_plan(m, acts);
+  if (rc) return rc;
+  if ((e = cudaMemcpyAsync(m->host_words, m->words, nwords * sizeof(unsigned), cudaMemcpyDeviceToHost, S(m))) !=
+      cudaSuccess)
+    return cuda_check(m->ctx, e, "readback");
+  return G3M3_OK;
+}
+
+// After the step's work completed: next time steps, div B when due.
+int step_finish(g3m3_model* m) {
+  cudaError_t e;
+  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(m->ctx, e, "main step");
+  finish_steps(m, 1, m->p.n_grids);
+  m->nsteps_done += 1;
+  if (m->p.divb_every > 0 && (m->nsteps_done % m->p.divb_every) == 0) {
+    const int st = g3m3_model_divb_all(m);
+    if (st && st != G3M3_ERR_NOCONV) return st;
+    if ((e = cudaStreamSynchronize(S(m))) != cudaSuccess) return cuda_check(m->ctx, e, "divb");
+  }
+  return G3M3_OK;
+}
+
 int copy_in(g3m3_model* m, float* dst, const float* src, size_t n) {
-  cudaError_t e = cudaMemcpyAsync(dst, src, n * sizeof(float), cudaMemcpyDefault, m->ctx->stream);
+  cudaError_t e = cudaMemcpyAsync(dst, src, n * sizeof(float), cudaMemcpyDefault, S(m));
   return e == cudaSuccess ? G3M3_OK : cuda_check(m->ctx, e, "cudaMemcpyAsync");
 }
 
@@ -574,6 +631,7 @@ int g3m3_model_create(g3m3_ctx* ctx, const g3m3_params* p, g3m3_model** out) {
     return set_err(ctx, G3M3_ERR_ARG, "bad model dimensions");
   g3m3_model* m = new g3m3_model();
   m->ctx = ctx;
+  m->stream = ctx->stream;
   m->p = *p;
   m->d = Dims{p->nx, p->ny, p->nz};
   m->n3 = m->d.cells();
@@ -589,7 +647,7 @@ int g3m3_model_create(g3m3_ctx* ctx, const g3m3_params* p, g3m3_model** out) {
 
 int g3m3_model_destroy(g3m3_model* m) {
   if (!m) return G3M3_ERR_ARG;
-  cudaStreamSynchronize(m->ctx->stream);
+  cudaStreamSynchronize(S(m));
   for (auto& kv : m->graphs) cudaGraphExecDestroy(kv.second);
   if (m->mem) cudaFree(m->mem);
   if (m->glist) cudaFree(m->glist);
@@ -603,11 +661,12 @@ int g3m3_model_destroy(g3m3_model* m) {
     if (m->ij[l]) cudaFree(m->ij[l]);
     if (m->parm[l]) cudaFree(m->parm[l]);
   }
+  if (m->own_stream) cudaStreamDestroy(m->stream);
   delete m;
   return G3M3_OK;
 }
 
-void* g3m3_model_stream(g3m3_model* m) { return m ? (void*)m->ctx->stream : nullptr; }
+void* g3m3_model_stream(g3m3_model* m) { return m ? (void*)S(m) : nullptr; }
 
 int g3m3_model_set_field(g3m3_model* m, int which, int field, const float* data) {
   if (!m || !data || field < 0 || field >= G3M3_NFIELDS || which < 0 || which > 2) return G3M3_ERR_ARG;
@@ -626,10 +685,10 @@ int g3m3_model_get_field(g3m3_model* m, int which, int field, float* data) {
   for (int b = 1; b <= m->p.n_grids; b++) {
     const float* src = which == 0 ? C(m, field, b) : (which == 1 ? O(m, field, b) : W(m, field, b));
     cudaError_t e = cudaMemcpyAsync(data + (size_t)(b - 1) * m->n3, src, m->n3 * sizeof(float), cudaMemcpyDefault,
-                                    m->ctx->stream);
+                                    S(m));
     if (e != cudaSuccess) return cuda_check(m->ctx, e, "get_field");
   }
-  cudaError_t e = cudaStreamSynchronize(m->ctx->stream);
+  cudaError_t e = cudaStreamSynchronize(S(m));
   return e == cudaSuccess ? G3M3_OK : cuda_check(m->ctx, e, "get_field sync");
 }
 
@@ -647,10 +706,10 @@ int g3m3_model_get_state(g3m3_model* m, float* data) {
   for (int f = 0; f < G3M3_NFIELDS; f++)
     for (int b = 1; b <= m->p.n_grids; b++) {
       cudaError_t e = cudaMemcpyAsync(data + (size_t)f * m->n4 + (size_t)(b - 1) * m->n3, C(m, f, b),
-                                      m->n3 * sizeof(float), cudaMemcpyDefault, m->ctx->stream);
+                                      m->n3 * sizeof(float), cudaMemcpyDefault, S(m));
       if (e != cudaSuccess) return cuda_check(m->ctx, e, "get_state");
     }
-  cudaError_t e = cudaStreamSynchronize(m->ctx->stream);
+  cudaError_t e = cudaStreamSynchronize(S(m));
   return e == cudaSuccess ? G3M3_OK : cuda_check(m->ctx, e, "get_state sync");
 }
 
@@ -735,9 +794,9 @@ int g3m3_model_init_steps(g3m3_model* m) {
     if (st) return st;
   }
   cudaError_t e = cudaMemcpyAsync(m->host_words, m->words, (8 + 5 * (size_t)G3M3_MAX_GRIDS) * sizeof(unsigned),
-                                  cudaMemcpyDeviceToHost, m->ctx->stream);
+                                  cudaMemcpyDeviceToHost, S(m));
   if (e != cudaSuccess) return cuda_check(m->ctx, e, "init readback");
-  if ((e = cudaStreamSynchronize(m->ctx->stream)) != cudaSuccess) return cuda_check(m->ctx, e, "init sync");
+  if ((e = cudaStreamSynchronize(S(m))) != cudaSuccess) return cuda_check(m->ctx, e, "init sync");
   finish_steps(m, 1, m->p.n_grids);
   return G3M3_OK;
 }
@@ -751,7 +810,7 @@ int g3m3_model_divb_all(g3m3_model* m) {
     for (int rep = 0; rep < 2; rep++) {
       int it = 0;
       int st = run_divb(m->ctx, C(m, G3M3_F_BX, b), C(m, G3M3_F_BY, b), C(m, G3M3_F_BZ, b), m->d, p.xspac[b - 1],
-                        p.divb_errlim, m->cg, m->host_cg, m->cgvec, m->ctx->stream, &it);
+                        p.divb_errlim, m->cg, m->host_cg, m->cgvec, S(m), &it);
       if (st == G3M3_ERR_NOCONV) worst = st;
       else if (st) return st;
     }
@@ -764,7 +823,7 @@ int g3m3_model_divb_all(g3m3_model* m) {
     a.nf = 3;
     fill_synced_geometry(a, m->d.nx, m->d.ny, m->d.nz, b, p.grd_xmin, p.grd_xmax, p.grd_ymin, p.grd_ymax,
                          p.grd_zmin, p.grd_zmax);
-    launch_flanks_synced(a, m->ctx->stream);
+    launch_flanks_synced(a, S(m));
   }
   for (int b = 1; b <= ng - 1; b++) corer_stage(m, b);
   cudaError_t e = cudaGetLastError();
@@ -776,37 +835,29 @@ int g3m3_model_run(g3m3_model* m, int nsteps, int use_graph) {
   if (!m || nsteps < 0) return G3M3_ERR_ARG;
   m->kernels = 0;
   m->graph_launches = 0;
-  const size_t nwords = 8 + 5 * (size_t)G3M3_MAX_GRIDS;
-  cudaStream_t s = m->ctx->stream;
+  cudaStream_t s = S(m);
   std::vector<Action> acts;
   for (int it = 0; it < nsteps; it++) {
-    const std::string roles = plan_key(m, {});
-    int rc = plan_main_step(m, acts);
+    std::string key;
+    int rc = step_plan(m, acts, key);
     if (rc) return rc;
-    std::string key = roles + plan_key(m, acts).substr(m->p.n_grids + 1);
     cudaError_t e;
-    m->launches_in_step = 0;
     if (use_graph) {
       auto found = m->graphs.find(key);
       if (found == m->graphs.end()) {
         // capture: scalar upload from the pinned table, the step, and the
         // read-back of the recorded maxima
-        int rcur[G3M3_MAX_GRIDS], rold[G3M3_MAX_GRIDS];
-        std::memcpy(rcur, m->role_cur, sizeof rcur);
-        std::memcpy(rold, m->role_old, sizeof rold);
+        Roles saved = save_roles(m);
         cudaGraph_t g = nullptr;
         if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
           return cuda_check(m->ctx, e, "begin capture");
-        cudaError_t e1 = cudaMemcpyAsync(m->d_scal, m->h_scal, m->scal_cap * sizeof(float), cudaMemcpyHostToDevice, s);
-        rc = enqueue_plan(m, acts);
-        cudaError_t e3 = cudaMemcpyAsync(m->host_words, m->words, nwords * sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+        rc = step_enqueue(m, acts);
         cudaError_t e2 = cudaStreamEndCapture(s, &g);
-        std::memcpy(m->role_cur, rcur, sizeof rcur);   // capture did not run anything
-        std::memcpy(m->role_old, rold, sizeof rold);
-        if (rc || e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
+        restore_roles(m, saved);   // capture did not run anything
+        if (rc || e2 != cudaSuccess) {
           if (g) cudaGraphDestroy(g);
           if (rc) return rc;
-          return cuda_check(m->ctx, e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3), "graph capture");
+          return cuda_check(m->ctx, e2, "graph capture");
         }
         cudaGraphExec_t ex = nullptr;
         e = cudaGraphInstantiate(&ex, g, 0);
@@ -820,24 +871,11 @@ int g3m3_model_run(g3m3_model* m, int nsteps, int use_graph) {
       m->graph_launches += 1;
       m->kernels += m->kernel_nodes[key];
     } else {
-      if ((e = cudaMemcpyAsync(m->d_scal, m->h_scal, (size_t)m->nscal * sizeof(float), cudaMemcpyHostToDevice, s)) !=
-          cudaSuccess)
-        return cuda_check(m->ctx, e, "scalar upload");
-      if ((rc = enqueue_plan(m, acts))) return rc;
-      if ((e = cudaMemcpyAsync(m->host_words, m->words, nwords * sizeof(unsigned), cudaMemcpyDeviceToHost, s)) !=
-          cudaSuccess)
-        return cuda_check(m->ctx, e, "readback");
+      if ((rc = step_enqueue(m, acts))) return rc;
       m->kernels += m->launches_in_step;
     }
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(m->ctx, e, "main step");
-    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(m->ctx, e, "main step");
-    finish_steps(m, 1, m->p.n_grids);
-    m->nsteps_done += 1;
-    if (m->p.divb_every > 0 && (m->nsteps_done % m->p.divb_every) == 0) {
-      const int st = g3m3_model_divb_all(m);
-      if (st && st != G3M3_ERR_NOCONV) return st;
-      if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(m->ctx, e, "divb");
-    }
+    if ((rc = step_finish(m))) return rc;
   }
   return G3M3_OK;
 }
@@ -966,7 +1004,7 @@ int g3m3_model_set_variant(g3m3_model* m, int kernel, int variant) {
 
 int g3m3_model_autotune(g3m3_model* m, int* fcs_variant) {
   if (!m) return G3M3_ERR_ARG;
-  cudaStream_t s = m->ctx->stream;
+  cudaStream_t s = S(m);
   const size_t n3 = m->n3;
   // scratch copies of box 1's current, old and wrk fields: timing runs on
   // realistic values without touching the state
@@ -1020,6 +1058,173 @@ int g3m3_model_stats(g3m3_model* m, int64_t* kernels, int64_t* graphs) {
   if (!m) return G3M3_ERR_ARG;
   if (kernels) *kernels = m->kernels;
   if (graphs) *graphs = m->graph_launches;
+  return G3M3_OK;
+}
+
+// --------------------------------------------------------------------------
+// Ensembles: independent states (e.g. one per upstream condition, boxes of
+// different sizes) advanced together.  Each member is a model with its own
+// stream.  In graph mode one main step of every member is captured into a
+// single CUDA graph -- fork from the ensemble's stream, each member's step on
+// its own stream, join -- so the members' kernels overlap on the GPU; the
+// graph is cached by the members' combined schedule key.  In plain mode the
+// members step one after another from the host loop.
+// --------------------------------------------------------------------------
+}  // extern "C"
+
+struct g3m3_ensemble {
+  g3m3_ctx* ctx = nullptr;
+  std::vector<g3m3_model*> members;
+  std::vector<cudaEvent_t> done;
+  cudaEvent_t fork = nullptr;
+  std::map<std::string, cudaGraphExec_t> graphs;
+  std::map<std::string, int64_t> kernel_nodes;
+  int64_t kernels = 0, graph_launches = 0;
+};
+
+extern "C" {
+
+int g3m3_ensemble_destroy(g3m3_ensemble* e) {
+  if (!e) return G3M3_ERR_ARG;
+  cudaStreamSynchronize(e->ctx->stream);
+  for (auto& kv : e->graphs) cudaGraphExecDestroy(kv.second);
+  for (g3m3_model* m : e->members) g3m3_model_destroy(m);
+  for (cudaEvent_t ev : e->done) cudaEventDestroy(ev);
+  if (e->fork) cudaEventDestroy(e->fork);
+  delete e;
+  return G3M3_OK;
+}
+
+int g3m3_ensemble_create(g3m3_ctx* ctx, int n, const g3m3_params* params, g3m3_ensemble** out) {
+  if (!ctx || !params || !out || n < 1) return G3M3_ERR_ARG;
+  *out = nullptr;
+  g3m3_ensemble* e = new g3m3_ensemble();
+  e->ctx = ctx;
+  cudaError_t ce = cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming);
+  for (int i = 0; i < n && ce == cudaSuccess; i++) {
+    g3m3_model* m = nullptr;
+    cudaStream_t st = nullptr;
+    if ((ce = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) != cudaSuccess) break;
+    const int rc = g3m3_model_create(ctx, &params[i], &m);
+    if (rc) {
+      cudaStreamDestroy(st);
+      g3m3_ensemble_destroy(e);
+      return rc;
+    }
+    // the model's set-up work ran on the context's stream
+    cudaStreamSynchronize(ctx->stream);
+    m->stream = st;
+    m->own_stream = true;
+    e->members.push_back(m);
+    cudaEvent_t ev = nullptr;
+    if ((ce = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) break;
+    e->done.push_back(ev);
+  }
+  if (ce != cudaSuccess) {
+    const int rc = cuda_check(ctx, ce, "ensemble create");
+    g3m3_ensemble_destroy(e);
+    return rc;
+  }
+  *out = e;
+  return G3M3_OK;
+}
+
+int g3m3_ensemble_member(g3m3_ensemble* e, int i, g3m3_model** out) {
+  if (!e || !out || i < 0 || i >= (int)e->members.size()) return G3M3_ERR_ARG;
+  *out = e->members[i];
+  return G3M3_OK;
+}
+
+void* g3m3_ensemble_stream(g3m3_ensemble* e) { return e ? (void*)e->ctx->stream : nullptr; }
+
+int g3m3_ensemble_run(g3m3_ensemble* e, int nsteps, int use_graph) {
+  if (!e || nsteps < 0) return G3M3_ERR_ARG;
+  const size_t nm = e->members.size();
+  cudaStream_t origin = e->ctx->stream;
+  e->kernels = 0;
+  e->graph_launches = 0;
+  std::vector<std::vector<Action>> acts(nm);
+  cudaError_t ce;
+  for (int it = 0; it < nsteps; it++) {
+    std::string key;
+    for (size_t i = 0; i < nm; i++) {
+      std::string k;
+      const int rc = step_plan(e->members[i], acts[i], k);
+      if (rc) return rc;
+      key += k;
+      key += '|';
+    }
+    // every member's step is ordered after earlier work on the ensemble's
+    // stream and the ensemble's stream after every member's step, so events
+    // recorded there bracket the whole step in both modes
+    auto fork_join = [&](bool capture_mode) -> int {
+      int64_t nk = 0;
+      if ((ce = cudaEventRecord(e->fork, origin)) != cudaSuccess) return cuda_check(e->ctx, ce, "fork");
+      for (size_t i = 0; i < nm; i++) {
+        g3m3_model* m = e->members[i];
+        if ((ce = cudaStreamWaitEvent(S(m), e->fork, 0)) != cudaSuccess) return cuda_check(e->ctx, ce, "fork");
+        const int rc = step_enqueue(m, acts[i]);
+        if (rc) return rc;
+        nk += m->launches_in_step;
+        if ((ce = cudaEventRecord(e->done[i], S(m))) != cudaSuccess) return cuda_check(e->ctx, ce, "join");
+        if ((ce = cudaStreamWaitEvent(origin, e->done[i], 0)) != cudaSuccess) return cuda_check(e->ctx, ce, "join");
+        if (!capture_mode) {
+          // plain mode: one member at a time, launched from the host loop
+          if ((ce = cudaStreamSynchronize(S(m))) != cudaSuccess) return cuda_check(e->ctx, ce, "member step");
+        }
+      }
+      e->kernels += capture_mode ? 0 : nk;
+      if (capture_mode) e->kernel_nodes[key] = nk;
+      return G3M3_OK;
+    };
+    if (use_graph) {
+      auto found = e->graphs.find(key);
+      if (found == e->graphs.end()) {
+        std::vector<Roles> saved(nm);
+        for (size_t i = 0; i < nm; i++) saved[i] = save_roles(e->members[i]);
+        cudaGraph_t g = nullptr;
+        if ((ce = cudaStreamBeginCapture(origin, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+          return cuda_check(e->ctx, ce, "begin capture");
+        const int rc = fork_join(true);
+        const cudaError_t e2 = cudaStreamEndCapture(origin, &g);
+        for (size_t i = 0; i < nm; i++) restore_roles(e->members[i], saved[i]);
+        if (rc || e2 != cudaSuccess) {
+          if (g) cudaGraphDestroy(g);
+          if (rc) return rc;
+          return cuda_check(e->ctx, e2, "graph capture");
+        }
+        cudaGraphExec_t ex = nullptr;
+        ce = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) return cuda_check(e->ctx, ce, "graph instantiate");
+        found = e->graphs.emplace(key, ex).first;
+      }
+      if ((ce = cudaGraphLaunch(found->second, origin)) != cudaSuccess) return cuda_check(e->ctx, ce, "graph launch");
+      for (size_t i = 0; i < nm; i++) apply_role_swaps(e->members[i], acts[i]);
+      e->graph_launches += 1;
+      e->kernels += e->kernel_nodes[key];
+    } else {
+      const int rc = fork_join(false);
+      if (rc) return rc;
+    }
+    if ((ce = cudaStreamSynchronize(origin)) != cudaSuccess) return cuda_check(e->ctx, ce, "ensemble step");
+    for (size_t i = 0; i < nm; i++) {
+      const int rc = step_finish(e->members[i]);
+      if (rc) return rc;
+    }
+  }
+  return G3M3_OK;
+}
+
+int g3m3_ensemble_stats(g3m3_ensemble* e, int64_t* kernels, int64_t* graphs, int64_t* cell_updates) {
+  if (!e) return G3M3_ERR_ARG;
+  if (kernels) *kernels = e->kernels;
+  if (graphs) *graphs = e->graph_launches;
+  if (cell_updates) {
+    int64_t cu = 0;
+    for (g3m3_model* m : e->members) cu += m->cell_updates;
+    *cell_updates = cu;
+  }
   return G3M3_OK;
 }
 

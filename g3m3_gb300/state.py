@@ -333,6 +333,23 @@ def make_config(name: str = "small", **over) -> State:
     return make_state(Setup(**kw))
 
 
+ENSEMBLE_LIMITS = (60, 48, 40)   # boxes of 121x121x61, 97x97x49, 81x81x41
+
+
+def ensemble_member(i: int, seed: int = 20261203, n_grids: int = 5, limits=ENSEMBLE_LIMITS, **over) -> State:
+    """Member i of the upstream-condition ensemble: box size cycling through
+    ``limits``, upstream wind drawn from the seed (n in [1,20] cm^-3, |v| in
+    [300,800] km/s, IMF clock angle in [0, 2 pi), |B| in [2,15] nT), the
+    nested-grid settings otherwise, and its own perturbation seed."""
+    rng = np.random.default_rng([seed, i])
+    wind = UpstreamWind(n_cm3=float(rng.uniform(1.0, 20.0)), speed_kms=float(rng.uniform(300.0, 800.0)),
+                        clock_angle=float(rng.uniform(0.0, 2.0 * math.pi)), b_nT=float(rng.uniform(2.0, 15.0)))
+    kw = dict(CONFIGS["nested"])
+    kw.update(limit=limits[i % len(limits)], n_grids=n_grids, wind=wind, seed=seed + 1000 + i)
+    kw.update(over)
+    return make_state(Setup(**kw))
+
+
 def perturbed(state: State, seed: int, scale: float = 1e-3) -> State:
     """A copy with every field multiplied by (1 + scale*N(0,1)) -- used to
     fill the old/wrk copies with data distinct from cur in kernel tests."""

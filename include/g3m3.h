@@ -52,6 +52,7 @@ extern "C" {
 
 typedef struct g3m3_ctx g3m3_ctx;
 typedef struct g3m3_model g3m3_model;
+typedef struct g3m3_ensemble g3m3_ensemble;
 
 /* ---- context -------------------------------------------------------- */
 int g3m3_ctx_create(g3m3_ctx** out, int device);
@@ -365,6 +366,27 @@ void* g3m3_model_stream(g3m3_model* m);
  * matters.  *bytes receives the algorithmic bytes of one launch. */
 int g3m3_model_time_kernel(g3m3_model* m, int kernel, int box, int reps,
     float* ms_per_launch, double* bytes);
+
+/* ---- ensembles ------------------------------------------------------
+ * n independent states (params[0..n-1]; box sizes may differ, e.g. one
+ * member per upstream condition) advanced together.  Each member is a
+ * g3m3_model with its own CUDA stream, set up with the g3m3_model_* calls
+ * through g3m3_ensemble_member (the ensemble owns and destroys it).
+ * g3m3_ensemble_run advances every member by nsteps main steps: with
+ * use_graph, one main step of all members is one CUDA graph (members on
+ * their own streams, overlapping on the GPU); without, the members step one
+ * after another from the host loop.  Results are those of running each
+ * member alone.  Work is ordered after earlier work on the ensemble's
+ * stream (the context's) and before later work there. */
+int g3m3_ensemble_create(g3m3_ctx* ctx, int n, const g3m3_params* params,
+    g3m3_ensemble** out);
+int g3m3_ensemble_destroy(g3m3_ensemble* e);
+int g3m3_ensemble_member(g3m3_ensemble* e, int i, g3m3_model** out);
+int g3m3_ensemble_run(g3m3_ensemble* e, int nsteps, int use_graph);
+/* Kernels and graphs launched by the last run; cell-updates of all members. */
+int g3m3_ensemble_stats(g3m3_ensemble* e, int64_t* kernels, int64_t* graphs,
+    int64_t* cell_updates);
+void* g3m3_ensemble_stream(g3m3_ensemble* e);
 
 #ifdef __cplusplus
 }
