@@ -115,28 +115,29 @@ int ensure_cg_scratch(g3m3_ctx* c, size_t cells) {
 // --------------------------------------------------------------------------
 // Shared pieces of the drop-in routines and the engine
 // --------------------------------------------------------------------------
-int run_divb(g3m3_ctx* c, float* bx, float* by, float* bz, const Dims& d, float rx, float errlim,
-             CgState* st, CgState* host_st, float* vec, cudaStream_t s, int* iters_out) {
-  DivbArgs a{};
-  a.bx = bx; a.by = by; a.bz = bz;
-  const size_t n = d.cells();
-  a.rhs = vec; a.x = vec + n; a.xs = vec + 2 * n; a.g = vec + 3 * n; a.h = vec + 4 * n;
-  a.xi = vec + 5 * n; a.xj = vec + 6 * n;
-  a.st = st; a.d = d; a.rx = rx; a.ry = rx; a.rz = rx;
+// The CG loop of sparse_solver (sub_sparse_solver.f90:19-159) on a prepared
+// argument block: initialise (from b = div B with x = 0, or from the
+// caller's x and b), iterate in chunks with the control decided on the
+// device, restart after a growing residual (the reference's recursive call,
+// :112-125) until the SAVEd restart count reaches 3.
+int run_cg(g3m3_ctx* c, const DivbArgs& a, float errlim, bool given, int redos0, CgState* host_st,
+           cudaStream_t s, int* iters_out, float* residual2_out, int* status_out) {
+  const size_t n = a.d.cells();
   CgState init{};
   const float e2 = (float)n * (errlim * errlim);   // sub_sparse_solver.f90:53 in FP32
   init.errlim2 = (double)e2;
   init.status = CG_RUNNING;
   init.maxit = (int)((10L * (long)n) > 2000000000L ? 2000000000L : 10L * (long)n);
-  init.redos = 1;
+  init.redos = redos0;
   *host_st = init;
-  G3M3_CUDA(c, cudaMemcpyAsync(st, host_st, sizeof(CgState), cudaMemcpyHostToDevice, s));
-  divb_launch_init(a, s);
+  G3M3_CUDA(c, cudaMemcpyAsync(a.st, host_st, sizeof(CgState), cudaMemcpyHostToDevice, s));
+  if (given) divb_launch_init_given(a, s);
+  else divb_launch_init(a, s);
   int status = CG_RUNNING;
   int chunk = 8;
   for (;;) {
     divb_launch_iterations(a, chunk, s);
-    G3M3_CUDA(c, cudaMemcpyAsync(host_st, st, sizeof(CgState), cudaMemcpyDeviceToHost, s));
+    G3M3_CUDA(c, cudaMemcpyAsync(host_st, a.st, sizeof(CgState), cudaMemcpyDeviceToHost, s));
     G3M3_CUDA(c, cudaStreamSynchronize(s));
     status = host_st->status;
     if (status == CG_RUNNING) {
@@ -155,14 +156,31 @@ int run_divb(g3m3_ctx* c, float* bx, float* by, float* bz, const Dims& d, float 
       h.redos += 1;
       h.status = CG_RUNNING;
       h.rsq = 0.0; h.anum = 0.0; h.aden = 0.0; h.r2 = 0.0; h.gg = 0.0; h.dgg = 0.0;
-      G3M3_CUDA(c, cudaMemcpyAsync(st, host_st, sizeof(CgState), cudaMemcpyHostToDevice, s));
+      G3M3_CUDA(c, cudaMemcpyAsync(a.st, host_st, sizeof(CgState), cudaMemcpyHostToDevice, s));
       divb_launch_restart(a, s);
       continue;
     }
     break;
   }
-  divb_launch_apply(a, s);
   if (iters_out) *iters_out = host_st->iters;
+  if (residual2_out) *residual2_out = (float)host_st->r2_last;
+  if (status_out) *status_out = status;
+  G3M3_CUDA(c, cudaGetLastError());
+  return G3M3_OK;
+}
+
+int run_divb(g3m3_ctx* c, float* bx, float* by, float* bz, const Dims& d, float rx, float errlim,
+             CgState* st, CgState* host_st, float* vec, cudaStream_t s, int* iters_out) {
+  DivbArgs a{};
+  a.bx = bx; a.by = by; a.bz = bz;
+  const size_t n = d.cells();
+  a.rhs = vec; a.x = vec + n; a.xs = vec + 2 * n; a.g = vec + 3 * n; a.h = vec + 4 * n;
+  a.xi = vec + 5 * n; a.xj = vec + 6 * n;
+  a.st = st; a.d = d; a.rx = rx; a.ry = rx; a.rz = rx;
+  int status = CG_RUNNING;
+  int rc = run_cg(c, a, errlim, false, 1, host_st, s, iters_out, nullptr, &status);
+  if (rc) return rc;
+  divb_launch_apply(a, s);
   G3M3_CUDA(c, cudaGetLastError());
   if (status == CG_MAXIT) return set_err(c, G3M3_ERR_NOCONV, "div B solver: too many iterations (%d)", host_st->iters);
   return G3M3_OK;
@@ -1014,6 +1032,40 @@ int g3m3_divb_correct(g3m3_ctx* ctx, int nx, int ny, int nz, int n_grids, int bo
   if (r.st) return r.st;
   return run_divb(ctx, dbx, dby, dbz, Dims{nx, ny, nz}, xs[box - 1], divb_errlim, ctx->cg, ctx->host_cg,
                   ctx->cgvec, ctx->stream, iters);
+}
+
+int g3m3_sparse_solver(g3m3_ctx* ctx, int nbands, int npts, const int* divb_band_pos, float divb_errlim,
+                       int recurse, int redo_lim, const float* divb, float* soln_vec, float* residual2,
+                       const float* banded_matrix) {
+  if (!ctx) return G3M3_ERR_ARG;
+  if (nbands < 1 || nbands > 16 || npts < 1 || !divb_band_pos)
+    return set_err(ctx, G3M3_ERR_ARG, "sparse_solver: nbands=%d (1..16), npts=%d", nbands, npts);
+  DivbArgs a{};
+  if (is_device_ptr(divb_band_pos))
+    G3M3_CUDA(ctx, cudaMemcpy(a.pos, divb_band_pos, nbands * sizeof(int), cudaMemcpyDeviceToHost));
+  else std::memcpy(a.pos, divb_band_pos, nbands * sizeof(int));
+  int s = ensure_cg_scratch(ctx, (size_t)npts);
+  if (s) return s;
+  Res r(ctx);
+  const size_t n = (size_t)npts;
+  a.rhs = r.f(divb, n);
+  a.x = r.f(soln_vec, n);
+  a.band = r.f(banded_matrix, (size_t)nbands * n);
+  if (r.st) return r.st;
+  float* vec = ctx->cgvec;
+  a.xs = vec; a.g = vec + n; a.h = vec + 2 * n; a.xi = vec + 3 * n; a.xj = vec + 4 * n;
+  a.st = ctx->cg;
+  a.d = Dims{npts, 1, 1};
+  a.nbands = nbands;
+  int status = CG_RUNNING;
+  // the SAVEd restart count starts at redo_lim for a recursive call (:55-60)
+  const int redos0 = (recurse ? redo_lim : 0) + 1;
+  float r2 = 0.0f;
+  s = run_cg(ctx, a, divb_errlim, true, redos0, ctx->host_cg, ctx->stream, nullptr, &r2, &status);
+  if (s) return s;
+  if (residual2) *residual2 = r2;
+  if (status == CG_MAXIT) return set_err(ctx, G3M3_ERR_NOCONV, "sparse_solver: too many iterations");
+  return G3M3_OK;
 }
 
 int g3m3_sample_points(g3m3_ctx* ctx, const float* field, int nx, int ny, int nz, int n_grids,

@@ -19,9 +19,16 @@ struct DivbArgs {
   CgState* st;
   Dims d;
   float rx, ry, rz;
+  // explicit banded operator (sparse_solver): band(nbands, n) column-major,
+  // product out(i) = sum_b band(b, i+pos[b]) x(i+pos[b]) (banded_tpose);
+  // null: the matrix-free 7-point Laplacian of d
+  const float* band;
+  int nbands;
+  int pos[16];
 };
 
 void divb_launch_init(const DivbArgs& a, cudaStream_t s);
+void divb_launch_init_given(const DivbArgs& a, cudaStream_t s);
 void divb_launch_restart(const DivbArgs& a, cudaStream_t s);
 void divb_launch_restore(const DivbArgs& a, cudaStream_t s);
 void divb_launch_iterations(const DivbArgs& a, int n, cudaStream_t s);

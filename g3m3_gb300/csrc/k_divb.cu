@@ -49,6 +49,18 @@ __device__ __forceinline__ float amul(const float* __restrict__ x, const Dims& d
   return r;
 }
 
+// the solver's matrix product (banded_tpose, sub_banded_tpose.f90:20-30)
+__device__ __forceinline__ float op(const DivbArgs& a, const float* __restrict__ x, size_t c, int i, int j, int k) {
+  if (a.band == nullptr) return amul(x, a.d, c, i, j, k);
+  const long long n = (long long)a.d.cells();
+  float r = 0.0f;
+  for (int b = 0; b < a.nbands; b++) {
+    const long long ii = (long long)c + a.pos[b];
+    if (ii >= 0 && ii < n) r = r + __ldg(a.band + (size_t)b + (size_t)a.nbands * (size_t)ii) * __ldg(x + ii);
+  }
+  return r;
+}
+
 __device__ __forceinline__ void ijk(size_t c, const Dims& d, int& i, int& j, int& k) {
   i = (int)(c % d.nx) + 1;
   const size_t r = c / d.nx;
@@ -91,13 +103,36 @@ __global__ void __launch_bounds__(TPB) k_cg_init(DivbArgs a) {
   }
 }
 
+// caller's iterate and right-hand side: xi = A x - b, bsq = |b|^2,
+// rsq = |xi|^2  (sub_sparse_solver.f90:61-71)
+__global__ void __launch_bounds__(TPB) k_cg_init_given(DivbArgs a) {
+  __shared__ double sh[TPB / 32];
+  const Dims d = a.d;
+  double bsq = 0.0, rsq = 0.0;
+  GRID_LOOP(c, d.cells()) {
+    int i, j, k;
+    ijk(c, d, i, j, k);
+    const float b = __ldg(a.rhs + c);
+    const float xi = op(a, a.x, c, i, j, k) - b;
+    a.xi[c] = xi;
+    bsq += (double)(b * b);
+    rsq += (double)(xi * xi);
+  }
+  bsq = block_sum(bsq, sh);
+  rsq = block_sum(rsq, sh);
+  if (threadIdx.x == 0) {
+    atomicAdd(&a.st->bsq, bsq);
+    atomicAdd(&a.st->rsq, rsq);
+  }
+}
+
 // g = -A xi ; h = g   (:73-75); also used after a restart
 __global__ void __launch_bounds__(TPB) k_cg_grad(DivbArgs a) {
   const Dims d = a.d;
   GRID_LOOP(c, d.cells()) {
     int i, j, k;
     ijk(c, d, i, j, k);
-    const float g = -amul(a.xi, d, c, i, j, k);
+    const float g = -op(a, a.xi, c, i, j, k);
     a.g[c] = g;
     a.h[c] = g;
   }
@@ -111,7 +146,7 @@ __global__ void __launch_bounds__(TPB) k_cg_resid(DivbArgs a) {
   GRID_LOOP(c, d.cells()) {
     int i, j, k;
     ijk(c, d, i, j, k);
-    const float xi = amul(a.x, d, c, i, j, k) - __ldg(a.rhs + c);
+    const float xi = op(a, a.x, c, i, j, k) - __ldg(a.rhs + c);
     a.xi[c] = xi;
     rsq += (double)(xi * xi);
   }
@@ -128,7 +163,7 @@ __global__ void __launch_bounds__(TPB) k_cg_a(DivbArgs a) {
   GRID_LOOP(c, d.cells()) {
     int i, j, k;
     ijk(c, d, i, j, k);
-    const float xi = amul(a.h, d, c, i, j, k);
+    const float xi = op(a, a.h, c, i, j, k);
     a.xi[c] = xi;
     an += (double)(__ldg(a.g + c) * __ldg(a.h + c));
     ad += (double)(xi * xi);
@@ -161,7 +196,7 @@ __global__ void __launch_bounds__(TPB) k_cg_c(DivbArgs a) {
   GRID_LOOP(c, d.cells()) {
     int i, j, k;
     ijk(c, d, i, j, k);
-    const float xj = amul(a.x, d, c, i, j, k) - __ldg(a.rhs + c);
+    const float xj = op(a, a.x, c, i, j, k) - __ldg(a.rhs + c);
     a.xj[c] = xj;
     r2 += (double)(xj * xj);
   }
@@ -197,7 +232,7 @@ __global__ void __launch_bounds__(TPB) k_cg_e(DivbArgs a) {
   GRID_LOOP(c, d.cells()) {
     int i, j, k;
     ijk(c, d, i, j, k);
-    const float xi = amul(a.xj, d, c, i, j, k);
+    const float xi = op(a, a.xj, c, i, j, k);
     a.xi[c] = xi;
     const float g = __ldg(a.g + c);
     gg += (double)(g * g);
@@ -268,6 +303,12 @@ unsigned cg_blocks(const Dims& d) {
 void divb_launch_init(const DivbArgs& a, cudaStream_t s) {
   const unsigned nb = cg_blocks(a.d);
   k_cg_init<<<nb, TPB, 0, s>>>(a);
+  k_cg_grad<<<nb, TPB, 0, s>>>(a);
+}
+
+void divb_launch_init_given(const DivbArgs& a, cudaStream_t s) {
+  const unsigned nb = cg_blocks(a.d);
+  k_cg_init_given<<<nb, TPB, 0, s>>>(a);
   k_cg_grad<<<nb, TPB, 0, s>>>(a);
 }
 

@@ -281,6 +281,21 @@ int g3m3_divb_correct(g3m3_ctx* ctx, int nx, int ny, int nz, int n_grids,
     int box, int nbands, const int* divb_band_pos, const float* xspac,
     float divb_errlim, float* bx, float* by, float* bz, int* iters);
 
+/* ---- a18: sparse_solver -- sub_sparse_solver.f90:19-20 ---------------
+ * CGNR on the banded system held in banded_matrix(nbands, npts) (column-
+ * major FP32, product as banded_tpose, sub_banded_tpose.f90:6-33:
+ * out(i) = sum_b banded_matrix(b, i+pos(b)) x(i+pos(b)), the matrix assumed
+ * symmetric as in the reference).  soln_vec is the starting iterate and
+ * receives the solution; residual2 receives |A x - divB|^2 of the last
+ * iterate.  recurse / redo_lim set the starting restart count as the
+ * reference's recursive call does (at most 3 restarts in all).  nbands <= 16.
+ * Dot products accumulate in FP64.  G3M3_ERR_NOCONV after 10*npts
+ * iterations (the reference only warns). */
+int g3m3_sparse_solver(g3m3_ctx* ctx, int nbands, int npts,
+    const int* divb_band_pos, float divb_errlim, int recurse, int redo_lim,
+    const float* divb, float* soln_vec, float* residual2,
+    const float* banded_matrix);
+
 /* ---- g3m3_divb_correct without device allocation (no counterpart in the
  * reference) ------------------------------------------------------------
  * Same arguments, arithmetic and results as g3m3_divb_correct, for callers

@@ -207,6 +207,13 @@ void oracle_flanks_synced(float* rho, int nx, int ny, int nz, int n_grids,
 /* ----- a18 div B ------------------------------------------------------- */
 /* Returns the iteration count of the outermost CG loop; x0 = 0 (the
  * reference's soln_vec is uninitialised stack memory). */
+/* sparse_solver (sub_sparse_solver.f90:19-159) on a caller's banded
+ * matrix, right-hand side and starting iterate; returns the iterations of
+ * the outermost call. */
+int oracle_sparse_solver(int nbands, int npts, const int* divb_band_pos,
+    float divb_errlim, int recurse, int redo_lim, const float* divb,
+    float* soln_vec, float* residual2, float* banded_matrix);
+
 int oracle_divb_correct(int nx, int ny, int nz, int n_grids, int box,
     int nbands, const int* divb_band_pos, const float* xspac,
     float divb_errlim, float* bx, float* by, float* bz);

@@ -286,6 +286,13 @@ done:
   return iters;
 }
 
+int oracle_sparse_solver(int nbands, int npts, const int* divb_band_pos,
+    float divb_errlim, int recurse, int redo_lim, const float* divb,
+    float* soln_vec, float* residual2, float* banded_matrix) {
+  return sparse_solver(nbands, npts, divb_band_pos, divb_errlim, recurse, redo_lim, divb, soln_vec, residual2,
+                       banded_matrix);
+}
+
 int oracle_divb_correct(int nx, int ny, int nz, int n_grids, int box,
     int nbands, const int* divb_band_pos, const float* xspac,
     float divb_errlim, float* bx_, float* by_, float* bz_) {

@@ -355,3 +355,41 @@ def test_sample_points():
         v = ctypes.c_float()
         oracle.call("trilin_interp", np.ascontiguousarray(xyz[t]), cube, q, ctypes.addressof(v))
         assert out[t] == v.value, (t, out[t], v.value)
+
+
+@pytest.mark.parametrize("recurse,redo_lim,x0", [(0, 0, 0.0), (1, 2, 0.3)])
+def test_sparse_solver(recurse, redo_lim, x0):
+    """Banded CGNR on a symmetric, diagonally dominant 7-band system, from a
+    zero or a random start; compared at the solver's tolerance (FP64 dot
+    products here, FP32 in the oracle)."""
+    from oracle import oracle
+    from g3m3_gb300.api import Context
+    nx = ny = nz = 11
+    n = nx * ny * nz
+    pos = np.array([nx * ny, nx, 1, 0, -1, -nx, -nx * ny], np.int32)
+    coef = np.array([1, 1, 1, -6.5, 1, 1, 1], np.float32)
+    bm = np.ascontiguousarray(np.repeat(coef[None, :], n, axis=0))   # banded_matrix(7, n), column-major
+    rng = np.random.default_rng(17)
+    b = rng.standard_normal(n).astype(np.float32)
+    start = (x0 * rng.standard_normal(n)).astype(np.float32)
+    errlim = 1e-6
+    xo = start.copy()
+    r2o = ctypes.c_float()
+    it_o = oracle.call("sparse_solver", 7, n, pos, errlim, recurse, redo_lim, b, xo, ctypes.addressof(r2o), bm)
+    xg = start.copy()
+    r2g = ctypes.c_float()
+    with Context() as ctx:
+        ctx.call("sparse_solver", 7, n, pos, errlim, recurse, redo_lim, b, xg, ctypes.addressof(r2g), bm)
+        ctx.sync_to_host(xg)
+    # the residual the library reports is the residual of its solution
+    def op(x):
+        out = np.zeros(n, np.float64)
+        for c, p in zip(coef, pos):
+            idx = np.arange(n) + p
+            ok = (idx >= 0) & (idx < n)
+            out[ok] += float(c) * x[idx[ok]]
+        return out
+    r2_true = float(np.sum((op(xg.astype(np.float64)) - b) ** 2))
+    assert r2_true <= 1.01 * float(np.sum(b.astype(np.float64) ** 2)) * n * errlim ** 2 * 1.5 + 1e-12
+    assert abs(r2g.value - r2_true) <= 0.05 * r2_true + 1e-10
+    assert rel_l2(xg, xo) < 1e-2, (rel_l2(xg, xo), it_o)
