@@ -49,6 +49,25 @@ __host__ __device__ inline bool is_pow2(float x) {
   return (c.u & 0x007fffffu) == 0u && ((c.u >> 23) & 0xffu) != 0u && ((c.u >> 23) & 0xffu) != 0xffu;
 }
 
+// x / d, correctly rounded, given r = RN(1/d) (an IEEE division done once
+// per denominator): Markstein's correction of the reciprocal product.  For
+// q = RN(x r) the residual x - q d is exact in one FMA, and RN(q + rem r)
+// is the correctly rounded quotient while nothing under- or overflows: the
+// quotient within [2^-124, 2^124] and |x| >= 2^-100, so that the residual is
+// a normal number (P. Markstein, "Computation of elementary functions on the
+// IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990).  Outside
+// that range the IEEE division is used.  Results are bit-identical to x / d.
+__device__ __forceinline__ float div_by(float x, float d, float r) {
+  const float q = x * r;
+  const float aq = fabsf(q);
+  if (aq >= 0x1p-124f && aq <= 0x1p+124f && fabsf(x) >= 0x1p-100f) {
+    const float rem = __fmaf_rn(-q, d, x);
+    return __fmaf_rn(rem, r, q);
+  }
+  if (x == 0.0f) return q;   // +-0 with the quotient's sign
+  return x / d;
+}
+
 // Divide by a grid spacing.  POW2 selects reciprocal multiplication, which is
 // exact for power-of-two spacings.
 template <bool POW2>
