@@ -158,6 +158,22 @@ class Model:
             addr(li["ijzero"]), addr(li["numzero"]), addr(li["parm_zero"]), li["ijzero"].shape[0]))
         self.ctx.synchronize()
 
+    def record_fluxes(self, scale, capacity: int):
+        """Record flux_counter of every box at the start of each main step
+        (scale: one float per box)."""
+        sc = np.ascontiguousarray(scale, np.float32)
+        self._flux_scale = sc
+        self.ctx.check(self.L.g3m3_model_record_fluxes(self.h, addr(sc), int(capacity)))
+        self._flux_cap = int(capacity)
+
+    def fluxes(self):
+        """(steps, n_grids, 6) array: q in, q out, h in, h out, o in, o out."""
+        cap = getattr(self, "_flux_cap", 0)
+        out = np.zeros((max(cap, 1), self.p.n_grids, 6), np.float32)
+        n = ctypes.c_int()
+        self.ctx.check(self.L.g3m3_model_fluxes(self.h, addr(out), ctypes.byref(n)))
+        return out[: n.value]
+
     def set_variant(self, kernel: int, variant: int):
         self.ctx.check(self.L.g3m3_model_set_variant(self.h, kernel, variant))
 

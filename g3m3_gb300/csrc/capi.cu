@@ -98,6 +98,14 @@ int ensure_guard_scratch(g3m3_ctx* c, size_t cells) {
   return G3M3_OK;
 }
 
+int ensure_words(g3m3_ctx* c) {
+  if (!c->words) {
+    G3M3_CUDA(c, cudaMalloc(&c->words, 16 * sizeof(unsigned)));
+    G3M3_CUDA(c, cudaMallocHost(&c->host_words, 16 * sizeof(unsigned)));
+  }
+  return G3M3_OK;
+}
+
 int ensure_cg_scratch(g3m3_ctx* c, size_t cells) {
   if (!c->cg) {
     G3M3_CUDA(c, cudaMalloc(&c->cg, sizeof(CgState)));
@@ -1032,6 +1040,37 @@ int g3m3_divb_correct(g3m3_ctx* ctx, int nx, int ny, int nz, int n_grids, int bo
   if (r.st) return r.st;
   return run_divb(ctx, dbx, dby, dbz, Dims{nx, ny, nz}, xs[box - 1], divb_errlim, ctx->cg, ctx->host_cg,
                   ctx->cgvec, ctx->stream, iters);
+}
+
+int g3m3_flux_counter(g3m3_ctx* ctx, const float* qpx, const float* qpy, const float* qpz, const float* hpx,
+                      const float* hpy, const float* hpz, const float* opx, const float* opy, const float* opz,
+                      int nx, int ny, int nz, int n_grids, int box, float rmassq, float rmassh, float rmasso,
+                      float grid_spacing, float* qflux_in, float* qflux_out, float* hflux_in, float* hflux_out,
+                      float* oflux_in, float* oflux_out) {
+  int s = check_dims(ctx, nx, ny, nz, n_grids, box);
+  if (s) return s;
+  if ((s = ensure_words(ctx))) return s;
+  const size_t n3 = (size_t)nx * ny * nz, n4 = n3 * n_grids, o = off(nx, ny, nz, box);
+  Res r(ctx);
+  FluxArgs a{};
+  const float* p[3][3] = {{qpx, qpy, qpz}, {hpx, hpy, hpz}, {opx, opy, opz}};
+  for (int sp = 0; sp < 3; sp++)
+    for (int q = 0; q < 3; q++) a.p[sp][q] = r.f(p[sp][q], n4) + o;
+  if (r.st) return r.st;
+  a.d = Dims{nx, ny, nz};
+  a.rmass[0] = rmassq; a.rmass[1] = rmassh; a.rmass[2] = rmasso;
+  a.grid_spacing = grid_spacing;
+  a.out = reinterpret_cast<float*>(ctx->words);
+  a.n_grids = n_grids; a.box = box;
+  launch_flux_counter(a, ctx->stream);
+  G3M3_CUDA(ctx, cudaMemcpyAsync(ctx->host_words, ctx->words, 6 * sizeof(float), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+  G3M3_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  const float* h = reinterpret_cast<const float*>(ctx->host_words);
+  float* outs[6] = {qflux_in, qflux_out, hflux_in, hflux_out, oflux_in, oflux_out};
+  for (int q = 0; q < 6; q++)
+    if (outs[q]) *outs[q] = h[q];
+  return finish(ctx, "flux_counter");
 }
 
 int g3m3_sparse_solver(g3m3_ctx* ctx, int nbands, int npts, const int* divb_band_pos, float divb_errlim,

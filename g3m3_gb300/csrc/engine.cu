@@ -72,6 +72,10 @@ struct g3m3_model {
   float iso_flag = 1.0f;
   int64_t kernels = 0, graph_launches = 0;
   int fcs_variant = 0;               // fcsmooth tile shape (g3m3_model_autotune)
+  float* flux_hist = nullptr;        // flux_counter history [step][box][6]
+  unsigned* flux_count = nullptr;
+  int flux_cap = 0;
+  float flux_scale[G3M3_MAX_GRIDS] = {};
   std::map<std::string, cudaGraphExec_t> graphs;
   std::map<std::string, int64_t> kernel_nodes;
   int64_t launches_in_step = 0;
@@ -592,6 +596,21 @@ int step_enqueue(g3m3_model* m, const std::vector<Action>& acts) {
   if ((e = cudaMemcpyAsync(m->d_scal, m->h_scal, m->scal_cap * sizeof(float), cudaMemcpyHostToDevice, S(m))) !=
       cudaSuccess)
     return cuda_check(m->ctx, e, "scalar upload");
+  if (m->flux_cap > 0) {
+    // flux_counter of every box at the start of the main step (3d_main.f90:1997-2011)
+    for (int b = m->p.n_grids; b >= 1; b--) {
+      FluxArgs fa{};
+      for (int sp = 0; sp < 3; sp++)
+        for (int q = 0; q < 3; q++) fa.p[sp][q] = C(m, 10 * sp + 1 + q, b);
+      fa.d = m->d;
+      fa.rmass[0] = m->p.rmassq; fa.rmass[1] = m->p.rmassh; fa.rmass[2] = m->p.rmasso;
+      fa.grid_spacing = m->flux_scale[b - 1];
+      fa.out = m->flux_hist; fa.count = m->flux_count; fa.capacity = (unsigned)m->flux_cap;
+      fa.n_grids = m->p.n_grids; fa.box = b; fa.advance = b == 1;
+      launch_flux_counter(fa, S(m));
+    }
+    m->launches_in_step += m->p.n_grids;
+  }
   int rc = enqueue_plan(m, acts);
   if (rc) return rc;
   if ((e = cudaMemcpyAsync(m->host_words, m->words, nwords * sizeof(unsigned), cudaMemcpyDeviceToHost, S(m))) !=
@@ -661,6 +680,8 @@ int g3m3_model_destroy(g3m3_model* m) {
     if (m->ij[l]) cudaFree(m->ij[l]);
     if (m->parm[l]) cudaFree(m->parm[l]);
   }
+  if (m->flux_hist) cudaFree(m->flux_hist);
+  if (m->flux_count) cudaFree(m->flux_count);
   if (m->own_stream) cudaStreamDestroy(m->stream);
   delete m;
   return G3M3_OK;
@@ -987,6 +1008,46 @@ int g3m3_model_time_kernel(g3m3_model* m, int kernel, int box, int reps, float* 
   if (e != cudaSuccess) return cuda_check(m->ctx, e, "time_kernel");
   *ms_per_launch = ms / (float)reps;
   if (bytes) *bytes = by;
+  return G3M3_OK;
+}
+
+int g3m3_model_record_fluxes(g3m3_model* m, const float* scale, int capacity) {
+  if (!m || capacity < 0 || (capacity > 0 && !scale)) return G3M3_ERR_ARG;
+  cudaStreamSynchronize(S(m));
+  if (m->flux_hist) cudaFree(m->flux_hist);
+  if (m->flux_count) cudaFree(m->flux_count);
+  m->flux_hist = nullptr;
+  m->flux_count = nullptr;
+  m->flux_cap = 0;
+  // the recording launches change the step's launch sequence
+  for (auto& kv : m->graphs) cudaGraphExecDestroy(kv.second);
+  m->graphs.clear();
+  m->kernel_nodes.clear();
+  if (capacity == 0) return G3M3_OK;
+  const size_t n = (size_t)capacity * m->p.n_grids * 6;
+  G3M3_CUDA(m->ctx, cudaMalloc(&m->flux_hist, n * sizeof(float)));
+  G3M3_CUDA(m->ctx, cudaMalloc(&m->flux_count, sizeof(unsigned)));
+  G3M3_CUDA(m->ctx, cudaMemsetAsync(m->flux_count, 0, sizeof(unsigned), S(m)));
+  G3M3_CUDA(m->ctx, cudaMemsetAsync(m->flux_hist, 0, n * sizeof(float), S(m)));
+  std::memcpy(m->flux_scale, scale, m->p.n_grids * sizeof(float));
+  m->flux_cap = capacity;
+  return G3M3_OK;
+}
+
+int g3m3_model_fluxes(g3m3_model* m, float* out, int* nsteps) {
+  if (!m) return G3M3_ERR_ARG;
+  unsigned n = 0;
+  if (m->flux_cap > 0) {
+    G3M3_CUDA(m->ctx, cudaMemcpyAsync(&n, m->flux_count, sizeof(unsigned), cudaMemcpyDeviceToHost, S(m)));
+    G3M3_CUDA(m->ctx, cudaStreamSynchronize(S(m)));
+    if (n > (unsigned)m->flux_cap) n = (unsigned)m->flux_cap;
+    if (out && n > 0) {
+      G3M3_CUDA(m->ctx, cudaMemcpyAsync(out, m->flux_hist, (size_t)n * m->p.n_grids * 6 * sizeof(float),
+                                        cudaMemcpyDeviceToHost, S(m)));
+      G3M3_CUDA(m->ctx, cudaStreamSynchronize(S(m)));
+    }
+  }
+  if (nsteps) *nsteps = (int)n;
   return G3M3_OK;
 }
 

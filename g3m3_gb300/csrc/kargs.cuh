@@ -144,6 +144,17 @@ struct ScatterArgs {
   unsigned int list_cap;
 };
 
+struct FluxArgs {           // flux_counter
+  const float* p[3][3];    // species (q, h, o) x momentum component (x, y, z), box slices
+  Dims d;
+  float rmass[3];
+  float grid_spacing;
+  float* out;              // 6 values (q in/out, h in/out, o in/out), or the history
+  unsigned int* count;     // history mode: slot counter of the main step (null: write out[0..5])
+  unsigned int capacity;   // history slots (main steps)
+  int n_grids, box, advance;   // advance: this launch moves the counter on
+};
+
 struct SampleArgs {
   const float* field;      // A(nx,ny,nz,n_grids)
   const float* xyz;        // (3,n)

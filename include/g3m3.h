@@ -281,6 +281,19 @@ int g3m3_divb_correct(g3m3_ctx* ctx, int nx, int ny, int nz, int n_grids,
     int box, int nbands, const int* divb_band_pos, const float* xspac,
     float divb_errlim, float* bx, float* by, float* bz, int* iters);
 
+/* ---- flux_counter -- sub_flux_counter.f90:5-8 -------------------------
+ * Ion momentum through the walls one cell inside the faces of box `box`,
+ * as inflow / outflow per species, scaled by grid_spacing / mass.  Each
+ * wall is summed in the reference's serial order, so the six results are
+ * the reference's bits; only they are copied back to the host. */
+int g3m3_flux_counter(g3m3_ctx* ctx, const float* qpx, const float* qpy,
+    const float* qpz, const float* hpx, const float* hpy, const float* hpz,
+    const float* opx, const float* opy, const float* opz,
+    int nx, int ny, int nz, int n_grids, int box,
+    float rmassq, float rmassh, float rmasso, float grid_spacing,
+    float* qflux_in, float* qflux_out, float* hflux_in, float* hflux_out,
+    float* oflux_in, float* oflux_out);
+
 /* ---- a18: sparse_solver -- sub_sparse_solver.f90:19-20 ---------------
  * CGNR on the banded system held in banded_matrix(nbands, npts) (column-
  * major FP32, product as banded_tpose, sub_banded_tpose.f90:6-33:
@@ -358,6 +371,15 @@ int g3m3_model_run(g3m3_model* m, int nsteps, int use_graph);
 /* div B cleaning of every box plus flanks_synced and bndry_corer
  * (3d_main.f90:3363-3408). */
 int g3m3_model_divb_all(g3m3_model* m);
+/* Flux history (flux_counter, 3d_main.f90:1996-2011): from the next run
+ * on, at the start of every main step the six fluxes of every box (boxes
+ * n_grids..1, scaled by scale[box-1]) are recorded on the device, up to
+ * `capacity` main steps; capacity 0 turns recording off.
+ * g3m3_model_fluxes copies the history out: out[step][box-1][6] as
+ * (q in, q out, h in, h out, o in, o out); *nsteps receives the steps
+ * recorded. */
+int g3m3_model_record_fluxes(g3m3_model* m, const float* scale, int capacity);
+int g3m3_model_fluxes(g3m3_model* m, float* out, int* nsteps);
 /* Tile shapes.  kernel 1 = fcsmooth: variant 0 = 32x8 tiles, 1 = 32x16.
  * Every variant gives the same bits; only the speed differs.
  * g3m3_model_autotune times each variant on scratch copies of box 1 (the

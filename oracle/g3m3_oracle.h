@@ -222,6 +222,15 @@ int oracle_divb_correct(int nx, int ny, int nz, int n_grids, int box,
 void oracle_findgrid(const float* xyz, int n_grids, const float* grid_minvals,
     const float* grid_maxvals, const float* xspac, int* gridpt,
     float re_equiv);
+/* flux_counter (sub_flux_counter.f90:5-158) */
+void oracle_flux_counter(const float* qpx, const float* qpy, const float* qpz,
+    const float* hpx, const float* hpy, const float* hpz,
+    const float* opx, const float* opy, const float* opz,
+    int nx, int ny, int nz, int n_grids, int box,
+    float rmassq, float rmassh, float rmasso, float grid_spacing,
+    float* qflux_in, float* qflux_out, float* hflux_in, float* hflux_out,
+    float* oflux_in, float* oflux_out);
+
 void oracle_trilin_interp(const float* sxyz, const float* gridpts,
     const float* qty, float* scdata);
 

@@ -1194,3 +1194,73 @@ void oracle_findgrid(const float* xyz, int n_grids, const float* grid_minvals,
     gridpt[d] = 1 + (int)(delta_pos / xspac[b - 1]);
   }
 }
+
+/* ======================================================================
+ * flux_counter (sub_flux_counter.f90:5-158): momentum summed over the
+ * walls one cell inside each face (index 2 and n-1), serially in the
+ * reference's loop order, then counted as inflow or outflow by the sign of
+ * the ionospheric-H+ sum.
+ * ==================================================================== */
+static void flux_wall(float f1[3], float f2[3], float* in[3], float* out[3],
+    const float gs, const float rm[3]) {
+  /* first wall: inflow when hflux1 > 0 (:48-56) */
+  if (f1[1] > 0) {
+    for (int s = 0; s < 3; s++) *in[s] = *in[s] + f1[s] * gs / rm[s];
+  } else {
+    for (int s = 0; s < 3; s++) *out[s] = *out[s] - f1[s] * gs / rm[s];
+  }
+  /* second wall: inflow when hflux2 < 0 (:58-66) */
+  if (f2[1] < 0) {
+    for (int s = 0; s < 3; s++) *in[s] = *in[s] - f2[s] * gs / rm[s];
+  } else {
+    for (int s = 0; s < 3; s++) *out[s] = *out[s] + f2[s] * gs / rm[s];
+  }
+}
+
+void oracle_flux_counter(const float* qpx, const float* qpy, const float* qpz,
+    const float* hpx, const float* hpy, const float* hpz,
+    const float* opx, const float* opy, const float* opz,
+    int nx, int ny, int nz, int n_grids, int box,
+    float rmassq, float rmassh, float rmasso, float grid_spacing,
+    float* qflux_in, float* qflux_out, float* hflux_in, float* hflux_out,
+    float* oflux_in, float* oflux_out) {
+  (void)n_grids;
+  const size_t n3 = (size_t)nx * ny * nz, o = (size_t)(box - 1) * n3;
+#define A(p, i, j, k) (p)[o + (size_t)((i) - 1) + (size_t)nx * ((size_t)((j) - 1) + (size_t)ny * (size_t)((k) - 1))]
+  const float rm[3] = {rmassq, rmassh, rmasso};
+  float* in[3] = {qflux_in, hflux_in, oflux_in};
+  float* out[3] = {qflux_out, hflux_out, oflux_out};
+  for (int s = 0; s < 3; s++) { *in[s] = 0.0f; *out[s] = 0.0f; }
+  const float* px[3] = {qpx, hpx, opx};
+  const float* py[3] = {qpy, hpy, opy};
+  const float* pz[3] = {qpz, hpz, opz};
+  float f1[3], f2[3];
+  /* x walls, i = 2 and nx-1 (:28-46) */
+  for (int s = 0; s < 3; s++) { f1[s] = 0.0f; f2[s] = 0.0f; }
+  for (int k = 1; k <= nz; k++)
+    for (int j = 1; j <= ny; j++)
+      for (int s = 0; s < 3; s++) {
+        f1[s] = f1[s] + A(px[s], 2, j, k);
+        f2[s] = f2[s] + A(px[s], nx - 1, j, k);
+      }
+  flux_wall(f1, f2, in, out, grid_spacing, rm);
+  /* y walls, j = 2 and ny-1 (:70-88) */
+  for (int s = 0; s < 3; s++) { f1[s] = 0.0f; f2[s] = 0.0f; }
+  for (int k = 1; k <= nz; k++)
+    for (int i = 1; i <= nx; i++)
+      for (int s = 0; s < 3; s++) {
+        f1[s] = f1[s] + A(py[s], i, 2, k);
+        f2[s] = f2[s] + A(py[s], i, ny - 1, k);
+      }
+  flux_wall(f1, f2, in, out, grid_spacing, rm);
+  /* z walls, k = 2 and nz-1 (:112-130) */
+  for (int s = 0; s < 3; s++) { f1[s] = 0.0f; f2[s] = 0.0f; }
+  for (int j = 1; j <= ny; j++)
+    for (int i = 1; i <= nx; i++)
+      for (int s = 0; s < 3; s++) {
+        f1[s] = f1[s] + A(pz[s], i, j, 2);
+        f2[s] = f2[s] + A(pz[s], i, j, nz - 1);
+      }
+  flux_wall(f1, f2, in, out, grid_spacing, rm);
+#undef A
+}

@@ -393,3 +393,30 @@ def test_sparse_solver(recurse, redo_lim, x0):
     assert r2_true <= 1.01 * float(np.sum(b.astype(np.float64) ** 2)) * n * errlim ** 2 * 1.5 + 1e-12
     assert abs(r2g.value - r2_true) <= 0.05 * r2_true + 1e-10
     assert rel_l2(xg, xo) < 1e-2, (rel_l2(xg, xo), it_o)
+
+
+@pytest.mark.parametrize("cfg,box", [("tiny2", 1), ("tiny2", 2), ("small", 1)])
+def test_flux_counter(cfg, box):
+    """Wall sums in the reference's serial order: the six fluxes are the
+    oracle's bits, for inflow and outflow walls alike."""
+    I = Inputs(cfg)
+    p = I.p
+    f = I.cur
+    rng = np.random.default_rng(23)
+    moms = []
+    for s in range(3):
+        for q in range(3):
+            a = f[10 * s + 1 + q].copy()
+            a += (0.3 * rng.standard_normal(a.shape)).astype(np.float32)   # both signs on every wall
+            moms.append(a)
+    args = moms + I.dims(box) + [p.rmassq, p.rmassh, p.rmasso, 1.7e3]
+    from oracle import oracle
+    from g3m3_gb300.api import Context
+    oo = [ctypes.c_float() for _ in range(6)]
+    oracle.call("flux_counter", *args, *[ctypes.addressof(x) for x in oo])
+    go = [ctypes.c_float() for _ in range(6)]
+    with Context() as ctx:
+        ctx.call("flux_counter", *args, *[ctypes.addressof(x) for x in go])
+    for x, y, n in zip(go, oo, ("q in", "q out", "h in", "h out", "o in", "o out")):
+        assert x.value == y.value, (n, x.value, y.value)
+    assert any(x.value != 0.0 for x in go)

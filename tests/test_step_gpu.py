@@ -102,3 +102,38 @@ def test_autotuned_steps():
     for q in range(34):
         assert_same(g[q], om.cur[q], f"mid3 field {q}")
     assert np.array_equal(tsn, om.t_stepnew)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_flux_history(graph):
+    """The engine records flux_counter of every box at the start of each
+    main step; the history matches the oracle applied to the oracle's state
+    at the same points."""
+    import ctypes
+    from oracle import oracle
+    from oracle.oracle import OracleModel
+    from g3m3_gb300.api import Context, Model
+    st = make_config("tiny3")
+    p = st.params
+    scale = np.array([1.0e3 * (b + 1) for b in range(p.n_grids)], np.float32)
+    om = OracleModel(st, omp=True)
+    om.init_steps()
+    nsteps = 3
+    want = np.zeros((nsteps, p.n_grids, 6), np.float32)
+    for n in range(nsteps):
+        for b in range(1, p.n_grids + 1):
+            oo = [ctypes.c_float() for _ in range(6)]
+            moms = [np.ascontiguousarray(om.cur[10 * s + 1 + q]) for s in range(3) for q in range(3)]
+            oracle.call("flux_counter", *moms, p.nx, p.ny, p.nz, p.n_grids, b, p.rmassq, p.rmassh, p.rmasso,
+                        float(scale[b - 1]), *[ctypes.addressof(x) for x in oo])
+            want[n, b - 1] = [x.value for x in oo]
+        assert om.main_step() == 0
+    with Context() as ctx:
+        m = Model(ctx, st)
+        m.record_fluxes(scale, 8)
+        m.init_steps()
+        m.run(nsteps, graph=graph)
+        got = m.fluxes()
+        m.close()
+    assert got.shape == want.shape
+    assert_same(got, want, "flux history")
