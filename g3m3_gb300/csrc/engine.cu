@@ -71,6 +71,8 @@ struct g3m3_model {
   int nsteps_done = 0;
   float iso_flag = 1.0f;
   int64_t kernels = 0, graph_launches = 0;
+  std::vector<int> h_ij[3];          // host copies of the inner-boundary tables (fluid files)
+  std::vector<float> h_parm[3];
   int fcs_variant = 0;               // fcsmooth tile shape (g3m3_model_autotune)
   float* flux_hist = nullptr;        // flux_counter history [step][box][6]
   unsigned* flux_count = nullptr;
@@ -775,6 +777,11 @@ int g3m3_model_set_inner(g3m3_model* m, const float* resistive, const int* ijsrf
     if ((e = cudaMemcpy(m->parm[l], parm[l], (size_t)mb * 7 * ml[l] * sizeof(float), cudaMemcpyDefault)) !=
         cudaSuccess)
       return cuda_check(m->ctx, e, "parms");
+    m->h_ij[l].assign(ij[l], ij[l] + (size_t)mb * 3 * ml[l]);
+    m->h_parm[l].resize((size_t)mb * 7 * ml[l]);
+    if ((e = cudaMemcpy(m->h_parm[l].data(), parm[l], m->h_parm[l].size() * sizeof(float), cudaMemcpyDefault)) !=
+        cudaSuccess)
+      return cuda_check(m->ctx, e, "parms");
   }
   // BandE's per-cell resistive coefficient: rst at the ijmid and ijzero
   // cells (sub_BandE.f90:191-219), 0 elsewhere
@@ -1008,6 +1015,57 @@ int g3m3_model_time_kernel(g3m3_model* m, int kernel, int box, int reps, float* 
   if (e != cudaSuccess) return cuda_check(m->ctx, e, "time_kernel");
   *ms_per_launch = ms / (float)reps;
   if (bytes) *bytes = by;
+  return G3M3_OK;
+}
+
+int g3m3_model_write_fluid(g3m3_model* m, const char* path) {
+  if (!m || !path) return G3M3_ERR_ARG;
+  if (m->h_ij[0].empty()) return set_err(m->ctx, G3M3_ERR_STATE, "write_fluid: inner-boundary tables not set");
+  const size_t n4 = m->n4;
+  std::vector<float> state((size_t)G3M3_NFIELDS * n4), b0(3 * n4);
+  int st = g3m3_model_get_state(m, state.data());
+  if (st) return st;
+  cudaError_t e = cudaMemcpyAsync(b0.data(), m->b0[0], 3 * n4 * sizeof(float), cudaMemcpyDeviceToHost, S(m));
+  if (e == cudaSuccess) e = cudaStreamSynchronize(S(m));
+  if (e != cudaSuccess) return cuda_check(m->ctx, e, "write_fluid");
+  const int mb = m->p.mbndry;
+  std::vector<int> num[3];
+  for (int l = 0; l < 3; l++) num[l].assign(m->num[l], m->num[l] + mb);
+  return g3m3_fluid_write(m->ctx, path, &m->p, m->t, state.data(), b0.data(), m->h_parm[0].data(),
+                          m->h_parm[1].data(), m->h_parm[2].data(), m->h_ij[2].data(), num[2].data(),
+                          m->h_ij[1].data(), num[1].data(), m->h_ij[0].data(), num[0].data(), m->mlen[0], m->mlen[1],
+                          m->mlen[2]);
+}
+
+int g3m3_model_read_fluid(g3m3_model* m, const char* path, int msrf, int mmid, int mzero) {
+  if (!m || !path || msrf < 1 || mmid < 1 || mzero < 1) return G3M3_ERR_ARG;
+  const size_t n4 = m->n4;
+  const int mb = m->p.mbndry;
+  std::vector<float> state((size_t)G3M3_NFIELDS * n4), b0(3 * n4);
+  std::vector<float> parm[3] = {std::vector<float>((size_t)mb * 7 * msrf), std::vector<float>((size_t)mb * 7 * mmid),
+                                std::vector<float>((size_t)mb * 7 * mzero)};
+  std::vector<int> ij[3] = {std::vector<int>((size_t)mb * 3 * msrf), std::vector<int>((size_t)mb * 3 * mmid),
+                            std::vector<int>((size_t)mb * 3 * mzero)};
+  std::vector<int> num[3] = {std::vector<int>(mb), std::vector<int>(mb), std::vector<int>(mb)};
+  double t = 0.0;
+  int st = g3m3_fluid_read(m->ctx, path, &m->p, &t, state.data(), b0.data(), parm[0].data(), parm[1].data(),
+                           parm[2].data(), ij[2].data(), num[2].data(), ij[1].data(), num[1].data(), ij[0].data(),
+                           num[0].data(), msrf, mmid, mzero);
+  if (st) return st;
+  if ((st = g3m3_model_set_state(m, state.data()))) return st;
+  // the wrk copy starts as the state (wrkepres is read before it is written)
+  for (int q = 0; q < G3M3_NFIELDS; q++)
+    if ((st = g3m3_model_set_field(m, 2, q, state.data() + (size_t)q * n4))) return st;
+  if ((st = g3m3_model_set_b0(m, b0.data(), b0.data() + n4, b0.data() + 2 * n4))) return st;
+  // the resistivity is not part of the file: keep the model's
+  std::vector<float> rst((size_t)mb * m->n3);
+  cudaError_t e = cudaMemcpy(rst.data(), m->resistive, rst.size() * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_check(m->ctx, e, "read_fluid");
+  if ((st = g3m3_model_set_inner(m, rst.data(), ij[0].data(), num[0].data(), parm[0].data(), msrf, ij[1].data(),
+                                 num[1].data(), parm[1].data(), mmid, ij[2].data(), num[2].data(), parm[2].data(),
+                                 mzero)))
+    return st;
+  m->t = t;
   return G3M3_OK;
 }
 

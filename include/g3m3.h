@@ -309,6 +309,32 @@ int g3m3_sparse_solver(g3m3_ctx* ctx, int nbands, int npts,
     const float* divb, float* soln_vec, float* residual2,
     const float* banded_matrix);
 
+/* ---- fluid files and state comparison -------------------------------
+ * The reference's fluid file: Fortran unformatted sequential records (a
+ * 4-byte little-endian byte count before and after each): t (real(dp));
+ * qrho qpx qpy qpz qpresx qpresy qpresz qpresxy qpresxz qpresyz, the same
+ * for h and o; bx by bz epres; bx0 by0 bz0 (each (nx,ny,nz,n_grids) FP32);
+ * then one record of parm_srf parm_mid parm_zero ijzero numzero ijmid
+ * nummid ijsrf numsrf (3d_main.f90:3305-3349, compare_fluids.f90).  Host
+ * arrays; state holds the 34 fields in g3m3_types.h order, b0 three fields.
+ * The table record is skipped on reading when parm_srf is NULL.  ctx may be
+ * NULL (no error text then); these two calls do not use the GPU. */
+int g3m3_fluid_write(g3m3_ctx* ctx, const char* path, const g3m3_params* p,
+    double t, const float* state, const float* b0, const float* parm_srf,
+    const float* parm_mid, const float* parm_zero, const int* ijzero,
+    const int* numzero, const int* ijmid, const int* nummid, const int* ijsrf,
+    const int* numsrf, int msrf, int mmid, int mzero);
+int g3m3_fluid_read(g3m3_ctx* ctx, const char* path, const g3m3_params* p,
+    double* t, float* state, float* b0, float* parm_srf, float* parm_mid,
+    float* parm_zero, int* ijzero, int* numzero, int* ijmid, int* nummid,
+    int* ijsrf, int* numsrf, int msrf, int mmid, int mzero);
+/* Field-by-field comparison of two states on the GPU (compare_fluids.f90's
+ * use): for each of nfields arrays a[f], b[f] of (nx,ny,nz,n_grids) and each
+ * box, stats[(f*n_grids + box-1)*4 + 0..3] = max |a-b|, sum (a-b)^2,
+ * sum a^2 (FP64), number of cells whose values differ (+0 = -0, NaN = NaN). */
+int g3m3_diff_fields(g3m3_ctx* ctx, int nfields, const float* const* a,
+    const float* const* b, int nx, int ny, int nz, int n_grids, double* stats);
+
 /* ---- g3m3_divb_correct without device allocation (no counterpart in the
  * reference) ------------------------------------------------------------
  * Same arguments, arithmetic and results as g3m3_divb_correct, for callers
@@ -371,6 +397,15 @@ int g3m3_model_run(g3m3_model* m, int nsteps, int use_graph);
 /* div B cleaning of every box plus flanks_synced and bndry_corer
  * (3d_main.f90:3363-3408). */
 int g3m3_model_divb_all(g3m3_model* m);
+/* Fluid (restart) files of the reference (3d_main.f90:3305-3349):
+ * g3m3_model_write_fluid writes the current state, b0 and the inner-boundary
+ * tables at the model's time t; g3m3_model_read_fluid loads them (cur and
+ * wrk copies, b0, tables; the resistivity stays the model's) and sets t.
+ * msrf/mmid/mzero are the table lengths the file was written with.  Call
+ * g3m3_model_init_steps after reading, as for a fresh state. */
+int g3m3_model_write_fluid(g3m3_model* m, const char* path);
+int g3m3_model_read_fluid(g3m3_model* m, const char* path, int msrf,
+    int mmid, int mzero);
 /* Flux history (flux_counter, 3d_main.f90:1996-2011): from the next run
  * on, at the start of every main step the six fluxes of every box (boxes
  * n_grids..1, scaled by scale[box-1]) are recorded on the device, up to
