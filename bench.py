@@ -212,7 +212,8 @@ def run_ours(args):
                    "cells_per_box": p.nx * p.ny * p.nz, "cell_updates_per_step": cu_g / args.steps / ws,
                    "mode": "one CUDA graph per main step", "l2": "working set (>400 MB per box) exceeds L2",
                    "parallelism": f"replicas x{ws}",
-                   "autotuned": {"fcsmooth_tile": "32x16" if fcs_variant == 1 else "32x8"}},
+                   "autotuned": {"fcsmooth": {0: "32x8 tiles", 1: "32x16 tiles",
+                                              2: "32x8 tiles, two fields per block, FP32x2"}[fcs_variant]}},
         "plain": {"value": cu_p / (ms_p / 1e3), "ms_per_step": ms_p / max(2, args.steps // 2),
                   "mode": "kernels launched from the host loop"},
         "e2e": {"value": cu_e / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": 34 * n4 * 4,

@@ -217,6 +217,257 @@ __global__ void __launch_bounds__(TX * TY) k_fcsmooth_tiled(const __grid_constan
   }
 }
 
+// ---- two fields per block, packed FP32x2 arithmetic -----------------
+// The same algorithm on a pair of fields: shared memory holds the two
+// fields' values interleaved, and the pair's FP32 adds and subtracts are
+// add/sub.rn.f32x2 (per-lane IEEE round-to-nearest, the scalar code's
+// operations in the same order).  Products that feed an add or subtract are
+// formed per lane with scalar mul.rn.f32: the code generator may contract a
+// packed multiply and a dependent packed add into one fused operation,
+// which would change the rounding.  Products that only feed the limiter's
+// min/max stay packed.  The limiter's sign, min and max act per lane.
+// Fewer FP32 instructions and half the shared-memory loads of the one-field
+// form for the same arithmetic.
+typedef unsigned long long f2x;
+
+__device__ __forceinline__ f2x pk(float a, float b) {
+  f2x r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void upk(f2x v, float& a, float& b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v)); }
+__device__ __forceinline__ f2x add2(f2x a, f2x b) {
+  f2x r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f2x sub2(f2x a, f2x b) {
+  f2x r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f2x mul2(f2x a, f2x b) {
+  f2x r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+// per-lane scalar products (never contracted with a following add)
+__device__ __forceinline__ f2x mul2s(f2x a, f2x b) {
+  float a0, a1, b0, b1;
+  upk(a, a0, a1);
+  upk(b, b0, b1);
+  return pk(a0 * b0, a1 * b1);
+}
+__device__ __forceinline__ f2x ld2(const float2* p) {
+  const float2 v = *p;
+  return pk(v.x, v.y);
+}
+
+__device__ __forceinline__ f2x limiter2(f2x dw, f2x d1m, f2x d1p, f2x chi) {
+  float dw0, dw1;
+  upk(dw, dw0, dw1);
+  const f2x s = pk(sign1(dw0), sign1(dw1));
+  float a0, a1, c0, c1, b0, b1;
+  upk(mul2(s, d1m), a0, a1);
+  upk(mul2(chi, pk(fabsf(dw0), fabsf(dw1))), c0, c1);
+  upk(mul2(s, d1p), b0, b1);
+  return mul2s(s, pk(amax1(0.0f, amin1(amin1(a0, c0), b0)), amax1(0.0f, amin1(amin1(a1, c1), b1))));
+}
+
+__device__ __forceinline__ f2x face_flux2(const float2* P, const float2* Wp, int o, int st, int m, int n, f2x chi) {
+  const f2x dw = sub2(ld2(Wp + o + st), ld2(Wp + o));
+  const f2x d1m = sub2(ld2(P + o), ld2(P + o - st));
+  const f2x d1p = (m + 1 <= n - 1) ? sub2(ld2(P + o + 2 * st), ld2(P + o + st)) : sub2(ld2(P + o + st), ld2(P + o));
+  return limiter2(dw, d1m, d1p, chi);
+}
+
+template <int TY>
+__global__ void __launch_bounds__(TX * TY, 2) k_fcsmooth_pair(const __grid_constant__ FcsArgs a) {
+  constexpr int NT = TX * TY;
+  constexpr int OX = TX + 6, OY = TY + 6;
+  constexpr int PX = TX + 4, PY = TY + 4;
+  constexpr int NO = OX * OY, NP = PX * PY;
+  constexpr int RO = (NO + NT - 1) / NT;
+  constexpr int RP = (NP + NT - 1) / NT;
+  __shared__ float2 sO[4][NO];
+  __shared__ float2 sW[4][NP];
+  __shared__ float2 sP[3][NP];
+  __shared__ float2 sFy[2][TY + 1][TX];
+  __shared__ float2 sFx[2][TY];
+  const Dims d = a.d;
+  const int f0 = 2 * blockIdx.z;
+  const bool two = f0 + 1 < a.nf;
+  const int f1 = two ? f0 + 1 : f0;
+  const float* __restrict__ W0 = a.wrk[f0];
+  const float* __restrict__ W1 = a.wrk[f1];
+  const float* __restrict__ O0 = a.old[f0];
+  const float* __restrict__ O1 = a.old[f1];
+  const f2x chi = pk(a.chi[f0], a.chi[f1]);
+  const f2x six = pk(6.0f, 6.0f);
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+  const int i0 = blockIdx.x * TX + 1, j0 = blockIdx.y * TY + 1;
+  const int gi = i0 + tx, gj = j0 + ty;
+  const bool mine = gi <= d.nx && gj <= d.ny;
+  const size_t plane = (size_t)d.nx * d.ny;
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+
+  int oofs[RO];
+#pragma unroll
+  for (int r = 0; r < RO; r++) {
+    const int t = tid + r * NT;
+    const int i = i0 - 3 + t % OX, j = j0 - 3 + t / OX;
+    oofs[r] = (t < NO && i >= 1 && i <= nx && j >= 1 && j <= ny) ? (j - 1) * nx + (i - 1) : -1;
+  }
+  int wofs[RP], pO[RP];
+  bool pedge[RP];
+#pragma unroll
+  for (int r = 0; r < RP; r++) {
+    const int t = tid + r * NT;
+    const int lx = t % PX, ly = t / PX;
+    const int i = i0 - 2 + lx, j = j0 - 2 + ly;
+    wofs[r] = (t < NP && i >= 1 && i <= nx && j >= 1 && j <= ny) ? (j - 1) * nx + (i - 1) : -1;
+    pO[r] = (ly + 1) * OX + lx + 1;
+    pedge[r] = i == 1 || i == nx || j == 1 || j == ny;
+  }
+  auto fetch_O = [&](int kp, float2* v) {
+#pragma unroll
+    for (int r = 0; r < RO; r++) {
+      v[r] = make_float2(0.0f, 0.0f);
+      if (kp >= 1 && kp <= nz && oofs[r] >= 0) {
+        const size_t c = (size_t)(kp - 1) * plane + oofs[r];
+        v[r] = make_float2(__ldg(O0 + c), __ldg(O1 + c));
+      }
+    }
+  };
+  auto fetch_W = [&](int kp, float2* v) {
+#pragma unroll
+    for (int r = 0; r < RP; r++) {
+      v[r] = make_float2(0.0f, 0.0f);
+      if (kp >= 1 && kp <= nz && wofs[r] >= 0) {
+        const size_t c = (size_t)(kp - 1) * plane + wofs[r];
+        v[r] = make_float2(__ldg(W0 + c), __ldg(W1 + c));
+      }
+    }
+  };
+  auto store_O = [&](int kp, const float2* v) {
+#pragma unroll
+    for (int r = 0; r < RO; r++)
+      if (tid + r * NT < NO) sO[kp & 3][tid + r * NT] = v[r];
+  };
+  auto store_W = [&](int kp, const float2* v) {
+#pragma unroll
+    for (int r = 0; r < RP; r++)
+      if (tid + r * NT < NP) sW[kp & 3][tid + r * NT] = v[r];
+  };
+
+  const int cc = (ty + 2) * PX + tx + 2;
+  const f2x z2 = pk(0.0f, 0.0f);
+  f2x p_m2 = z2, p_m1 = z2, p_0 = z2, p_p1 = z2, p_p2 = z2;
+  f2x w_m1 = z2, w_0 = z2, w_p1 = z2;
+  f2x fx_cur = z2, fy_cur = z2, fz_prev = z2;
+  float2 rO[RO], rW[RP];
+
+  fetch_O(1, rO); store_O(1, rO);
+  fetch_O(2, rO); store_O(2, rO);
+  fetch_W(1, rW); store_W(1, rW);
+  __syncthreads();
+  for (int kf = 1; kf <= nz + 2; kf++) {
+    fetch_O(kf + 2, rO);
+    fetch_W(kf + 1, rW);
+    if (kf <= nz) {
+      float2* dP = sP[kf % 3];
+      const float2* Wk = sW[kf & 3];
+      const float2* Om = sO[(kf - 1) & 3];
+      const float2* Oc = sO[kf & 3];
+      const float2* Op = sO[(kf + 1) & 3];
+      const bool zb = kf == 1 || kf == nz;
+#pragma unroll
+      for (int r = 0; r < RP; r++) {
+        const int t = tid + r * NT;
+        if (t < NP) {
+          f2x v = z2;
+          if (wofs[r] >= 0) {
+            const f2x w = ld2(Wk + t);
+            if (zb || pedge[r]) {
+              v = w;
+            } else {
+              const int q = pO[r];
+              const f2x sum = add2(add2(add2(add2(add2(ld2(Oc + q + 1), ld2(Oc + q - 1)), ld2(Oc + q + OX)),
+                                                ld2(Oc + q - OX)),
+                                           ld2(Op + q)),
+                                      ld2(Om + q));
+              v = add2(w, mul2s(chi, sub2(sum, mul2s(six, ld2(Oc + q)))));
+            }
+          }
+          float lo, hi;
+          upk(v, lo, hi);
+          dP[t] = make_float2(lo, hi);
+        }
+      }
+    }
+    const int kx = kf - 1;
+    f2x fx_next = z2, fy_next = z2;
+    if (kx >= 2 && kx <= nz - 1) {
+      const float2* P = sP[kx % 3];
+      const float2* Wp = sW[kx & 3];
+      fx_next = face_flux2(P, Wp, cc, 1, gi, nx, chi);
+      fy_next = face_flux2(P, Wp, cc, PX, gj, ny, chi);
+      float lo, hi;
+      upk(fy_next, lo, hi);
+      sFy[kx & 1][ty + 1][tx] = make_float2(lo, hi);
+      if (ty == 0) {
+        upk(face_flux2(P, Wp, cc - PX, PX, j0 - 1, ny, chi), lo, hi);
+        sFy[kx & 1][0][tx] = make_float2(lo, hi);
+      } else if (ty == 1 && tx < TY) {
+        upk(face_flux2(P, Wp, (tx + 2) * PX + 1, 1, i0 - 1, nx, chi), lo, hi);
+        sFx[kx & 1][tx] = make_float2(lo, hi);
+      }
+    }
+    __syncthreads();
+    const int k = kf - 2;
+    p_m2 = p_m1; p_m1 = p_0; p_0 = p_p1; p_p1 = p_p2;
+    p_p2 = (kf <= nz) ? ld2(sP[kf % 3] + cc) : z2;
+    w_m1 = w_0; w_0 = w_p1;
+    w_p1 = (k + 1 >= 1 && k + 1 <= nz) ? ld2(sW[(k + 1) & 3] + cc) : z2;
+    const f2x fx_left_lane = __shfl_up_sync(0xffffffffu, fx_cur, 1);
+    if (mine && k >= 1) {
+      const size_t c = (size_t)(k - 1) * plane + (size_t)(gj - 1) * nx + (gi - 1);
+      f2x res;
+      if (k == 1 || k == nz) {
+        res = w_0;
+      } else {
+        const float2* P = sP[k % 3];
+        const float2* Wp = sW[k & 3];
+        f2x tv;
+        if (gi == 1 || gi == nx) {
+          tv = ld2(Wp + cc);
+        } else {
+          const f2x fl = gi == 2 ? fx_cur : (tx == 0 ? ld2(&sFx[k & 1][ty]) : fx_left_lane);
+          tv = add2(sub2(ld2(P + cc), fx_cur), fl);
+        }
+        if (gj != 1 && gj != ny) {
+          const f2x fl = gj == 2 ? fy_cur : ld2(&sFy[k & 1][ty][tx]);
+          tv = add2(sub2(tv, fy_cur), fl);
+        }
+        const f2x d1p_k = (k + 1 <= nz - 1) ? sub2(p_p2, p_p1) : sub2(p_p1, p_0);
+        const f2x fz0 = limiter2(sub2(w_p1, w_0), sub2(p_0, p_m1), d1p_k, chi);
+        const f2x fz1 = k == 2 ? fz0 : fz_prev;
+        fz_prev = fz0;
+        res = add2(sub2(tv, fz0), fz1);
+      }
+      float lo, hi;
+      upk(res, lo, hi);
+      a.px[f0][c] = lo;
+      if (two) a.px[f1][c] = hi;
+    }
+    fx_cur = fx_next;
+    fy_cur = fy_next;
+    store_O(kf + 2, rO);
+    store_W(kf + 1, rW);
+    __syncthreads();
+  }
+}
+
 }  // namespace
 
 template <int TY>
@@ -226,9 +477,19 @@ static void launch_ty(const FcsArgs& a, cudaStream_t s) {
   k_fcsmooth_tiled<TY><<<grd, blk, 0, s>>>(a);
 }
 
-// variant 0: 32x8 tiles, 1: 32x16 tiles
+template <int TY>
+static void launch_pair(const FcsArgs& a, cudaStream_t s) {
+  const dim3 blk(TX, TY, 1);
+  const dim3 grd((unsigned)((a.d.nx + TX - 1) / TX), (unsigned)((a.d.ny + TY - 1) / TY),
+                 (unsigned)((a.nf + 1) / 2));
+  k_fcsmooth_pair<TY><<<grd, blk, 0, s>>>(a);
+}
+
+// variant 0: 32x8 tiles, 1: 32x16 tiles, 2: 32x8 tiles with two fields per
+// block in packed FP32x2 arithmetic
 void launch_fcsmooth_tiled(const FcsArgs& a, cudaStream_t s, int variant) {
   if (variant == 1) launch_ty<16>(a, s);
+  else if (variant == 2) launch_pair<8>(a, s);
   else launch_ty<8>(a, s);
 }
 

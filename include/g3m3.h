@@ -415,7 +415,8 @@ int g3m3_model_read_fluid(g3m3_model* m, const char* path, int msrf,
  * recorded. */
 int g3m3_model_record_fluxes(g3m3_model* m, const float* scale, int capacity);
 int g3m3_model_fluxes(g3m3_model* m, float* out, int* nsteps);
-/* Tile shapes.  kernel 1 = fcsmooth: variant 0 = 32x8 tiles, 1 = 32x16.
+/* Tile shapes.  kernel 1 = fcsmooth: variant 0 = 32x8 tiles, 1 = 32x16,
+ * 2 = 32x8 tiles with two fields per block in packed FP32x2 arithmetic.
  * Every variant gives the same bits; only the speed differs.
  * g3m3_model_autotune times each variant on scratch copies of box 1 (the
  * state is not changed), keeps the fastest and reports it; cached step
