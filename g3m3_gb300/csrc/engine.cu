@@ -78,6 +78,12 @@ struct g3m3_model {
   unsigned* flux_count = nullptr;
   int flux_cap = 0;
   float flux_scale[G3M3_MAX_GRIDS] = {};
+  float* craft_traj = nullptr;       // virtual spacecraft: trajectories (4, samples)
+  int* craft_start = nullptr;        // first sample of each craft
+  float* craft_out = nullptr;        // records [step][craft][4 + nf]
+  unsigned* craft_count = nullptr;
+  int ncraft = 0, craft_nf = 0, craft_cap = 0, craft_t_slot = -1;
+  int craft_fields[8] = {};
   std::map<std::string, cudaGraphExec_t> graphs;
   std::map<std::string, int64_t> kernel_nodes;
   int64_t launches_in_step = 0;
@@ -586,6 +592,8 @@ int step_plan(g3m3_model* m, std::vector<Action>& acts, std::string& key) {
   int rc = plan_main_step(m, acts);
   if (rc) return rc;
   key = roles + plan_key(m, acts).substr(m->p.n_grids + 1);
+  // the step's time for the spacecraft records (t advanced by the plan)
+  m->craft_t_slot = m->craft_cap > 0 ? scal_slot(m, (float)m->t) : -1;
   return G3M3_OK;
 }
 
@@ -615,6 +623,24 @@ int step_enqueue(g3m3_model* m, const std::vector<Action>& acts) {
   }
   int rc = enqueue_plan(m, acts);
   if (rc) return rc;
+  if (m->craft_cap > 0 && m->craft_t_slot >= 0) {
+    // virtual spacecraft at the end of the step (cft_craft_handling.f90:120-200)
+    CraftArgs ca{};
+    const g3m3_params& p = m->p;
+    ca.geo.n_grids = p.n_grids; ca.geo.d = m->d; ca.geo.re_equiv = p.re_equiv;
+    for (int b = 0; b < p.n_grids; b++) {
+      ca.geo.gmin[3 * b] = p.grd_xmin[b]; ca.geo.gmin[3 * b + 1] = p.grd_ymin[b]; ca.geo.gmin[3 * b + 2] = p.grd_zmin[b];
+      ca.geo.gmax[3 * b] = p.grd_xmax[b]; ca.geo.gmax[3 * b + 1] = p.grd_ymax[b]; ca.geo.gmax[3 * b + 2] = p.grd_zmax[b];
+      ca.geo.xspac[b] = p.xspac[b];
+    }
+    ca.traj = m->craft_traj; ca.start = m->craft_start; ca.ncraft = m->ncraft; ca.nf = m->craft_nf;
+    for (int f = 0; f < m->craft_nf; f++)
+      for (int b = 1; b <= p.n_grids; b++) ca.fld[f][b - 1] = C(m, m->craft_fields[f], b);
+    ca.t = sref(m, m->craft_t_slot);
+    ca.out = m->craft_out; ca.count = m->craft_count; ca.capacity = (unsigned)m->craft_cap;
+    launch_craft(ca, S(m));
+    m->launches_in_step += 1;
+  }
   if ((e = cudaMemcpyAsync(m->host_words, m->words, nwords * sizeof(unsigned), cudaMemcpyDeviceToHost, S(m))) !=
       cudaSuccess)
     return cuda_check(m->ctx, e, "readback");
@@ -684,6 +710,10 @@ int g3m3_model_destroy(g3m3_model* m) {
   }
   if (m->flux_hist) cudaFree(m->flux_hist);
   if (m->flux_count) cudaFree(m->flux_count);
+  if (m->craft_traj) cudaFree(m->craft_traj);
+  if (m->craft_start) cudaFree(m->craft_start);
+  if (m->craft_out) cudaFree(m->craft_out);
+  if (m->craft_count) cudaFree(m->craft_count);
   if (m->own_stream) cudaStreamDestroy(m->stream);
   delete m;
   return G3M3_OK;
@@ -1066,6 +1096,63 @@ int g3m3_model_read_fluid(g3m3_model* m, const char* path, int msrf, int mmid, i
                                  mzero)))
     return st;
   m->t = t;
+  return G3M3_OK;
+}
+
+int g3m3_model_record_craft(g3m3_model* m, int ncraft, const int* npts, const float* traj, int nf,
+                            const int* fields, int capacity) {
+  if (!m || ncraft < 0 || ncraft > 128 || nf < 0 || nf > 8 || capacity < 0) return G3M3_ERR_ARG;
+  if (capacity > 0 && (ncraft < 1 || nf < 1 || !npts || !traj || !fields)) return G3M3_ERR_ARG;
+  cudaStreamSynchronize(S(m));
+  float** bufs[3] = {&m->craft_traj, &m->craft_out, nullptr};
+  for (int q = 0; q < 2; q++)
+    if (*bufs[q]) { cudaFree(*bufs[q]); *bufs[q] = nullptr; }
+  if (m->craft_start) { cudaFree(m->craft_start); m->craft_start = nullptr; }
+  if (m->craft_count) { cudaFree(m->craft_count); m->craft_count = nullptr; }
+  m->craft_cap = 0;
+  m->ncraft = 0;
+  // the recording launch changes the step's launch sequence
+  for (auto& kv : m->graphs) cudaGraphExecDestroy(kv.second);
+  m->graphs.clear();
+  m->kernel_nodes.clear();
+  if (capacity == 0) return G3M3_OK;
+  std::vector<int> start(ncraft + 1, 0);
+  for (int c = 0; c < ncraft; c++) {
+    if (npts[c] < 1) return set_err(m->ctx, G3M3_ERR_ARG, "craft %d has no trajectory samples", c);
+    start[c + 1] = start[c] + npts[c];
+  }
+  for (int f = 0; f < nf; f++) {
+    if (fields[f] < 0 || fields[f] >= G3M3_NFIELDS) return set_err(m->ctx, G3M3_ERR_ARG, "bad field index");
+    m->craft_fields[f] = fields[f];
+  }
+  const size_t nrec = (size_t)capacity * ncraft * (4 + nf);
+  G3M3_CUDA(m->ctx, cudaMalloc(&m->craft_traj, (size_t)4 * start[ncraft] * sizeof(float)));
+  G3M3_CUDA(m->ctx, cudaMalloc(&m->craft_start, (ncraft + 1) * sizeof(int)));
+  G3M3_CUDA(m->ctx, cudaMalloc(&m->craft_out, nrec * sizeof(float)));
+  G3M3_CUDA(m->ctx, cudaMalloc(&m->craft_count, sizeof(unsigned)));
+  G3M3_CUDA(m->ctx, cudaMemcpy(m->craft_traj, traj, (size_t)4 * start[ncraft] * sizeof(float), cudaMemcpyDefault));
+  G3M3_CUDA(m->ctx, cudaMemcpy(m->craft_start, start.data(), (ncraft + 1) * sizeof(int), cudaMemcpyHostToDevice));
+  G3M3_CUDA(m->ctx, cudaMemset(m->craft_count, 0, sizeof(unsigned)));
+  m->ncraft = ncraft;
+  m->craft_nf = nf;
+  m->craft_cap = capacity;
+  return G3M3_OK;
+}
+
+int g3m3_model_craft_records(g3m3_model* m, float* out, int* nsteps) {
+  if (!m) return G3M3_ERR_ARG;
+  unsigned n = 0;
+  if (m->craft_cap > 0) {
+    G3M3_CUDA(m->ctx, cudaMemcpyAsync(&n, m->craft_count, sizeof(unsigned), cudaMemcpyDeviceToHost, S(m)));
+    G3M3_CUDA(m->ctx, cudaStreamSynchronize(S(m)));
+    if (n > (unsigned)m->craft_cap) n = (unsigned)m->craft_cap;
+    if (out && n > 0) {
+      G3M3_CUDA(m->ctx, cudaMemcpyAsync(out, m->craft_out, (size_t)n * m->ncraft * (4 + m->craft_nf) * sizeof(float),
+                                        cudaMemcpyDeviceToHost, S(m)));
+      G3M3_CUDA(m->ctx, cudaStreamSynchronize(S(m)));
+    }
+  }
+  if (nsteps) *nsteps = (int)n;
   return G3M3_OK;
 }
 

@@ -165,4 +165,16 @@ struct SampleArgs {
   float re_equiv;
 };
 
+struct CraftArgs {          // per-step virtual-spacecraft recording
+  SampleArgs geo;           // grid description (field, xyz, out, n unused)
+  const float* traj;        // (4, samples): x, y, z in planet radii, t
+  const int* start;         // first sample of each craft, ncraft + 1 entries
+  int ncraft, nf;
+  const float* fld[8][G3M3_MAX_GRIDS];   // box slices of the recorded fields
+  ScalarRef t;              // model time after the step
+  float* out;               // [capacity][ncraft][4 + nf]
+  unsigned int* count;
+  unsigned int capacity;
+};
+
 }  // namespace g3m3

@@ -415,6 +415,20 @@ int g3m3_model_read_fluid(g3m3_model* m, const char* path, int msrf,
  * recorded. */
 int g3m3_model_record_fluxes(g3m3_model* m, const float* scale, int capacity);
 int g3m3_model_fluxes(g3m3_model* m, float* out, int* nsteps);
+/* Virtual spacecraft (cft_craft_handling.f90:120-200): ncraft <= 128
+ * trajectories, craft c with npts[c] samples (x, y, z in planet radii, t in
+ * the model's time units) sorted by t, all in traj(4, sum npts).  From the
+ * next run on, at the end of every main step each craft's position at the
+ * model time is interpolated between the samples around it (linterp,
+ * cft_linterp.f90) and the fields `fields[0..nf-1]` (nf <= 8, indices of
+ * g3m3_types.h) are sampled trilinearly in the smallest box holding it,
+ * on the device, up to `capacity` steps; capacity 0 stops recording.
+ * g3m3_model_craft_records copies out records [step][craft][4 + nf] =
+ * (t, x, y, z, values); a craft whose trajectory does not cover t records
+ * NaN. */
+int g3m3_model_record_craft(g3m3_model* m, int ncraft, const int* npts,
+    const float* traj, int nf, const int* fields, int capacity);
+int g3m3_model_craft_records(g3m3_model* m, float* out, int* nsteps);
 /* Tile shapes.  kernel 1 = fcsmooth: variant 0 = 32x8 tiles, 1 = 32x16,
  * 2 = 32x8 tiles with two fields per block in packed FP32x2 arithmetic.
  * Every variant gives the same bits; only the speed differs.

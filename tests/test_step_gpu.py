@@ -3,6 +3,8 @@ restatement of the reference main loop (3d_main.f90:1925-3095) on nested,
 sub-cycled boxes -- after 1 and after N main steps, host-loop launches and
 CUDA-graph replay alike.  Bitwise: the engine performs the reference's FP32
 operations in the reference's order."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -138,3 +140,75 @@ def test_flux_history(graph):
         m.close()
     assert got.shape == want.shape
     assert_same(got, want, "flux history")
+
+
+def _oracle_sample(field, xyz, p):
+    """findgrid + trilin_interp of the oracle at one point (field: (n_grids, nz, ny, nx))."""
+    import ctypes
+    from oracle import oracle
+    gmin = np.array([[p.grd_xmin[b], p.grd_ymin[b], p.grd_zmin[b]] for b in range(p.n_grids)], np.float32)
+    gmax = np.array([[p.grd_xmax[b], p.grd_ymax[b], p.grd_zmax[b]] for b in range(p.n_grids)], np.float32)
+    xs = np.array(p.xspac[: p.n_grids], np.float32)
+    gp = (ctypes.c_int * 4)()
+    pt = np.ascontiguousarray(xyz, np.float32)
+    oracle.call("findgrid", pt, p.n_grids, gmin, gmax, xs, gp, p.re_equiv)
+    i, j, k, b = gp[0], gp[1], gp[2], gp[3]
+    cube = np.zeros((2, 3), np.float32)
+    for a in range(3):
+        cube[0, a] = (gmin[b - 1, a] + np.float32(gp[a] - 1) * xs[b - 1]) * np.float32(p.re_equiv)
+        cube[1, a] = cube[0, a] + xs[b - 1] * np.float32(p.re_equiv)
+    q = np.ascontiguousarray(field[b - 1, k - 1:k + 1, j - 1:j + 1, i - 1:i + 1])
+    v = ctypes.c_float()
+    oracle.call("trilin_interp", pt, cube, q, ctypes.addressof(v))
+    return v.value
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_craft_records(graph):
+    """Virtual spacecraft recorded on the device at the end of each main
+    step: positions interpolated along the trajectories (FP32, as linterp),
+    values equal to the oracle's findgrid + trilin_interp on the model's
+    state of that step; a craft outside its time range records NaN."""
+    from g3m3_gb300.api import Context, Model
+    st = make_config("tiny3")
+    p = st.params
+    f32 = np.float32
+    # three trajectories in planet radii: through the inner box, across the
+    # middle box, and one that starts only after the second step
+    tr = [np.array([[-2.0, -1.5, 0.3, 0.0], [2.5, 1.0, -0.4, 50.0]], np.float32),
+          np.array([[5.0, -4.0, 1.0, 0.0], [0.0, 0.0, 0.0, 1.0], [-6.0, 3.0, -1.0, 60.0]], np.float32),
+          np.array([[1.0, 1.0, 0.5, 1e6], [1.5, 1.0, 0.5, 2e6]], np.float32)]
+    npts = np.array([len(t) for t in tr], np.int32)
+    traj = np.ascontiguousarray(np.concatenate(tr).reshape(-1), np.float32)
+    fields = np.array([31, 32, 33, 0], np.int32)
+    nsteps = 3
+    states, times = [], []
+    with Context() as ctx:
+        m = Model(ctx, st)
+        ctx.check(ctx.L.g3m3_model_record_craft(m.h, len(tr), npts.ctypes.data, traj.ctypes.data, len(fields),
+                                                fields.ctypes.data, 8))
+        m.init_steps()
+        for _ in range(nsteps):
+            m.run(1, graph=graph)
+            states.append(m.state())
+            times.append(m.times()[0])
+        rec = np.zeros((8, len(tr), 4 + len(fields)), np.float32)
+        n = ctypes.c_int()
+        ctx.check(ctx.L.g3m3_model_craft_records(m.h, rec.ctypes.data, ctypes.byref(n)))
+        m.close()
+    assert n.value == nsteps
+    for s_ in range(nsteps):
+        t = f32(times[s_])
+        for c, T in enumerate(tr):
+            r = rec[s_, c]
+            assert r[0] == t
+            seg = [i for i in range(len(T) - 1) if T[i, 3] <= t < T[i + 1, 3]]
+            if not seg:
+                assert np.isnan(r[1:]).all()
+                continue
+            x1, x2 = T[seg[0]], T[seg[0] + 1]
+            xyz = np.array([x1[q] + (x2[q] - x1[q]) / (x2[3] - x1[3]) * (t - x1[3]) for q in range(3)], np.float32)
+            assert np.array_equal(r[1:4], xyz), (s_, c, r[1:4], xyz)
+            for fi, fq in enumerate(fields):
+                want = _oracle_sample(states[s_][fq], xyz, p)
+                assert r[4 + fi] == want, (s_, c, fq, r[4 + fi], want)
