@@ -39,6 +39,8 @@ def ctype_of(param: str):
     p = " ".join(param.replace("const", " ").split())
     if "*" in p or "[" in p:
         return ctypes.c_void_p
+    if p.startswith("unsigned long long"):
+        return ctypes.c_ulonglong
     base = p.split()[0]
     if base in ("int32_t",):
         return ctypes.c_int32

@@ -122,13 +122,14 @@ class Context:
 class Model:
     """A multi-box state on the device advanced by the step engine."""
 
-    def __init__(self, ctx: Context, state, handle=None):
+    def __init__(self, ctx: Context, state, handle=None, params=None):
         """A new model for ``state``; with ``handle``, a view of a model the
         library already holds (an ensemble member), which this object loads
-        with ``state`` but does not destroy."""
+        with ``state`` but does not destroy.  With ``state`` None, an empty
+        model for ``params`` (fill it with :meth:`init_state`)."""
         self.ctx = ctx
         self.L = ctx.L
-        self.p = state.params
+        self.p = state.params if state is not None else params
         self.owned = handle is None
         if handle is None:
             h = ctypes.c_void_p()
@@ -137,7 +138,14 @@ class Model:
             ctx._models.append(self)
         else:
             self.h = handle
-        self.upload(state)
+        if state is not None:
+            self.upload(state)
+
+    def init_state(self, alf_inner=-5.0, seed=20261203, noise=0.01, iono_lo=1.0, iono_hi=1.0):
+        """The fresh-start state built on the device (dipole, plasma load,
+        solar wind, speed clip, seeded perturbation, inner lists)."""
+        self.ctx.check(self.L.g3m3_model_init_state(self.h, float(alf_inner), int(seed), float(noise),
+                                                   float(iono_lo), float(iono_hi)))
 
     def upload(self, state):
         L, h = self.L, self.h

@@ -12,7 +12,9 @@
 //  * the time-dependent scalars of a main step (dt/2, dt, flank time
 //    weights) live in a small device table, so that one captured CUDA graph
 //    replays every main step with the same schedule shape.
+#include <array>
 #include <cmath>
+#include <algorithm>
 #include <cstring>
 #include <map>
 #include <string>
@@ -1097,6 +1099,122 @@ int g3m3_model_read_fluid(g3m3_model* m, const char* path, int msrf, int mmid, i
     return st;
   m->t = t;
   return G3M3_OK;
+}
+
+int g3m3_model_init_state(g3m3_model* m, float alf_inner, unsigned long long seed, float noise, float iono_lo,
+                          float iono_hi) {
+  if (!m || noise < 0.0f || !(iono_lo > 0.0f) || iono_hi < iono_lo) return G3M3_ERR_ARG;
+  const g3m3_params& p = m->p;
+  const int nx = p.nx, ny = p.ny, nz = p.nz, mb = p.mbndry;
+  const double r_inner = p.r_inner;
+  const double zero_b = r_inner - 1.5, mid_b = r_inner - 0.5, srf_b = r_inner + 0.6;
+  const double b0c = (double)alf_inner * std::sqrt((double)p.erho) * (r_inner * r_inner * r_inner);
+  const double xdip = 0.00001;
+  // per-cell fields of every box on the device
+  for (int b = 1; b <= p.n_grids; b++) {
+    InitArgs a{};
+    for (int q = 0; q < G3M3_NFIELDS; q++) a.f[q] = C(m, q, b);
+    for (int q = 0; q < 3; q++) a.b0[q] = m->b0[q] + (size_t)(b - 1) * m->n3;
+    a.d = m->d; a.box = b;
+    a.xmin = p.grd_xmin[b - 1]; a.ymin = p.grd_ymin[b - 1]; a.zmin = p.grd_zmin[b - 1];
+    a.dx = ((double)p.grd_xmax[b - 1] - p.grd_xmin[b - 1]) / (nx - 1.0);
+    a.dy = ((double)p.grd_ymax[b - 1] - p.grd_ymin[b - 1]) / (ny - 1.0);
+    a.dz = ((double)p.grd_zmax[b - 1] - p.grd_zmin[b - 1]) / (nz - 1.0);
+    a.b0c = b0c; a.zero_b = zero_b; a.re_equiv = p.re_equiv; a.r_rot = p.r_rot; a.v_rot = p.v_rot;
+    a.r_inner = r_inner; a.alpha_e = p.alpha_e; a.erho = p.erho; a.d_min = 0.01; a.cs_inner = 0.0163;
+    a.ti_te = p.ti_te; a.gamma = p.gamma; a.spress = p.spress; a.srho = p.srho;
+    a.spx = p.spx; a.spy = p.spy; a.spz = p.spz; a.rho_frac = p.rho_frac;
+    a.rmass[0] = p.rmassq; a.rmass[1] = p.rmassh; a.rmass[2] = p.rmasso;
+    a.noise = noise; a.seed = seed;
+    launch_init(a, S(m));
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_check(m->ctx, e, "init_state");
+  // the wrk copy starts as the state (wrkepres is read before it is written)
+  for (int q = 0; q < G3M3_NFIELDS; q++)
+    for (int b = 1; b <= p.n_grids; b++)
+      if ((e = cudaMemcpyAsync(W(m, q, b), C(m, q, b), m->n3 * sizeof(float), cudaMemcpyDeviceToDevice, S(m))) !=
+          cudaSuccess)
+        return cuda_check(m->ctx, e, "init_state");
+  // inner-boundary lists of boxes <= mbndry (3d_main.f90:1374-1452), in the
+  // reference's loop order, with the cell's density and pressure values
+  const int parm_fields[7] = {0, 10, 20, 4, 14, 24, G3M3_F_EPRES};
+  std::vector<int> ij[3];
+  std::vector<float> parm[3];
+  std::vector<int> nums[3];
+  std::vector<std::vector<std::array<int, 3>>> cells(3 * mb);
+  std::vector<std::vector<std::array<float, 7>>> vals(3 * mb);
+  std::vector<float> host((size_t)7 * m->n3);
+  for (int b = 1; b <= mb; b++) {
+    for (int q = 0; q < 7; q++)
+      if ((e = cudaMemcpyAsync(host.data() + (size_t)q * m->n3, C(m, parm_fields[q], b), m->n3 * sizeof(float),
+                               cudaMemcpyDeviceToHost, S(m))) != cudaSuccess)
+        return cuda_check(m->ctx, e, "init_state");
+    if ((e = cudaStreamSynchronize(S(m))) != cudaSuccess) return cuda_check(m->ctx, e, "init_state");
+    const double dx = ((double)p.grd_xmax[b - 1] - p.grd_xmin[b - 1]) / (nx - 1.0);
+    const double dy = ((double)p.grd_ymax[b - 1] - p.grd_ymin[b - 1]) / (ny - 1.0);
+    const double dz = ((double)p.grd_zmax[b - 1] - p.grd_zmin[b - 1]) / (nz - 1.0);
+    for (int k = 0; k < nz; k++)
+      for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+          const double ax = (double)p.grd_xmin[b - 1] + dx * i - xdip;
+          const double ay = (double)p.grd_ymin[b - 1] + dy * j;
+          const double az = (double)p.grd_zmin[b - 1] + dz * k;
+          const double ar = std::sqrt(ax * ax + ay * ay + az * az);
+          if (!(ar <= srf_b)) continue;
+          const int l = ar < zero_b ? 2 : (ar < mid_b ? 1 : 0);   // 0 srf, 1 mid, 2 zero
+          const size_t c = (size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k);
+          std::array<float, 7> v;
+          for (int q = 0; q < 7; q++) v[q] = host[(size_t)q * m->n3 + c];
+          cells[3 * (b - 1) + l].push_back({i + 1, j + 1, k + 1});
+          vals[3 * (b - 1) + l].push_back(v);
+        }
+  }
+  // ionospheric inflow densities, log-uniform per list entry
+  unsigned long long rs = seed ^ 0x5851f42d4c957f2dull;
+  auto uni = [&]() {
+    rs += 0x9e3779b97f4a7c15ull;
+    unsigned long long z = rs;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return (double)((z ^ (z >> 31)) >> 11) * 0x1p-53;
+  };
+  for (int l = 0; l < 3; l++)
+    for (int b = 1; b <= mb; b++)
+      for (auto& v : vals[3 * (b - 1) + l]) {
+        const double f = iono_hi > iono_lo
+                             ? std::exp(std::log((double)iono_lo) + uni() * (std::log((double)iono_hi) - std::log((double)iono_lo)))
+                             : 1.0;
+        for (int q = 0; q < 3; q++) v[q] = (float)(v[q] * f);
+      }
+  int ml[3];
+  for (int l = 0; l < 3; l++) {
+    ml[l] = 1;
+    for (int b = 1; b <= mb; b++) ml[l] = std::max(ml[l], (int)cells[3 * (b - 1) + l].size());
+    ij[l].assign((size_t)mb * 3 * ml[l], 0);
+    parm[l].assign((size_t)mb * 7 * ml[l], 0.0f);
+    nums[l].assign(mb, 0);
+    for (int b = 1; b <= mb; b++) {
+      const auto& cl = cells[3 * (b - 1) + l];
+      const auto& vl = vals[3 * (b - 1) + l];
+      nums[l][b - 1] = (int)cl.size();
+      for (size_t n = 0; n < cl.size(); n++) {
+        for (int q = 0; q < 3; q++) ij[l][(b - 1) + (size_t)mb * (q + 3 * n)] = cl[n][q];
+        for (int q = 0; q < 7; q++) parm[l][(b - 1) + (size_t)mb * (q + 7 * n)] = vl[n][q];
+      }
+    }
+  }
+  // set_resist with b0 = 1 (sub_set_resist.f90:10-63)
+  std::vector<float> rst((size_t)mb * m->n3, 0.0f);
+  const float rval[3] = {0.125f / p.resist, 0.5f / p.resist, 1.0f / p.resist};
+  for (int l : {2, 1, 0})
+    for (int b = 1; b <= mb; b++)
+      for (const auto& c3 : cells[3 * (b - 1) + l])
+        rst[(size_t)(b - 1) * m->n3 + (size_t)(c3[0] - 1) + (size_t)nx * ((size_t)(c3[1] - 1) + (size_t)ny * (c3[2] - 1))] =
+            rval[l];
+  return g3m3_model_set_inner(m, rst.data(), ij[0].data(), nums[0].data(), parm[0].data(), ml[0], ij[1].data(),
+                              nums[1].data(), parm[1].data(), ml[1], ij[2].data(), nums[2].data(), parm[2].data(),
+                              ml[2]);
 }
 
 int g3m3_model_record_craft(g3m3_model* m, int ncraft, const int* npts, const float* traj, int nf,

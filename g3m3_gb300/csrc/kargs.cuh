@@ -165,6 +165,19 @@ struct SampleArgs {
   float re_equiv;
 };
 
+struct InitArgs {           // fresh-start state of one box (k_init.cu)
+  float* f[G3M3_NFIELDS];
+  float* b0[3];
+  Dims d;
+  int box;
+  float xmin, ymin, zmin;
+  double dx, dy, dz;
+  double b0c, zero_b, re_equiv, r_rot, v_rot, r_inner, alpha_e, erho, d_min, cs_inner, ti_te, gamma;
+  double spress, srho, spx, spy, spz, rho_frac, rmass[3];
+  float noise;
+  unsigned long long seed;
+};
+
 struct CraftArgs {          // per-step virtual-spacecraft recording
   SampleArgs geo;           // grid description (field, xyz, out, n unused)
   const float* traj;        // (4, samples): x, y, z in planet radii, t

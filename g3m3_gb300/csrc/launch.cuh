@@ -18,6 +18,7 @@ inline unsigned blocks_for(size_t n, unsigned threads) {
 // k_push.cu
 void launch_flux_counter(const FluxArgs& a, cudaStream_t s);
 void launch_craft(const CraftArgs& a, cudaStream_t s);
+void launch_init(const InitArgs& a, cudaStream_t s);
 void launch_push_ion(const PushIonArgs& a, cudaStream_t s);
 void launch_push_field(const PushFieldArgs& a, cudaStream_t s);
 // k_fields.cu

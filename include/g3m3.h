@@ -415,6 +415,17 @@ int g3m3_model_read_fluid(g3m3_model* m, const char* path, int msrf,
  * recorded. */
 int g3m3_model_record_fluxes(g3m3_model* m, const float* scale, int capacity);
 int g3m3_model_fluxes(g3m3_model* m, float* out, int* nsteps);
+/* Fresh-start state built on the device (3d_main.f90:1268-1629): dipole
+ * background of strength alf_inner (moment along -z when negative),
+ * corotating ionospheric plasma, the solar-wind fill from the params'
+ * upstream values, the speed clip, a seeded multiplicative perturbation of
+ * density and diagonal pressures (relative size `noise`, counter-based
+ * normals from `seed`), the inner-boundary lists of boxes <= mbndry with
+ * ionospheric densities scaled log-uniformly in [iono_lo, iono_hi], and the
+ * resistivity shells.  Replaces g3m3_model_set_state/set_b0/set_inner for a
+ * fresh start; call g3m3_model_init_steps next. */
+int g3m3_model_init_state(g3m3_model* m, float alf_inner,
+    unsigned long long seed, float noise, float iono_lo, float iono_hi);
 /* Virtual spacecraft (cft_craft_handling.f90:120-200): ncraft <= 128
  * trajectories, craft c with npts[c] samples (x, y, z in planet radii, t in
  * the model's time units) sorted by t, all in traj(4, sum npts).  From the
