@@ -141,6 +141,20 @@ class Model:
         if state is not None:
             self.upload(state)
 
+    GRAPHING = (["bx_total", "by_total", "bz_total", "btot", "ex", "ey", "ez", "jx", "jy", "jz"]
+                + [f"{s}{q}" for s in ("q", "h", "o")
+                   for q in ("vx", "vy", "vz", "p_para", "p_perp", "p_cross", "rho")] + ["epres"])
+
+    def graphing(self, box: int, plane: int, index: int):
+        """One grid plane (0: x-y at k=index, 1: x-z at j=index, 2: y-z at
+        i=index) of the graphing quantities of box ``box``, code units."""
+        p = self.p
+        na = p.ny if plane == 0 else p.nz
+        nb = p.ny if plane == 2 else p.nx
+        out = np.zeros((32, na, nb), np.float32)
+        self.ctx.check(self.L.g3m3_model_graphing(self.h, box, plane, index, addr(out)))
+        return dict(zip(self.GRAPHING, out))
+
     def init_state(self, alf_inner=-5.0, seed=20261203, noise=0.01, iono_lo=1.0, iono_hi=1.0):
         """The fresh-start state built on the device (dipole, plasma load,
         solar wind, speed clip, seeded perturbation, inner lists)."""

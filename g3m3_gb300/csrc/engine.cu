@@ -1101,6 +1101,46 @@ int g3m3_model_read_fluid(g3m3_model* m, const char* path, int msrf, int mmid, i
   return G3M3_OK;
 }
 
+int g3m3_model_graphing(g3m3_model* m, int box, int plane, int index, float* out) {
+  if (!m || !out || box < 1 || box > m->p.n_grids || plane < 0 || plane > 2) return G3M3_ERR_ARG;
+  const Dims d = m->d;
+  const int lim = plane == 0 ? d.nz : (plane == 1 ? d.ny : d.nx);
+  if (index < 1 || index > lim) return set_err(m->ctx, G3M3_ERR_ARG, "graphing: plane index %d outside 1..%d", index, lim);
+  const int na = plane == 0 ? d.ny : d.nz, nb = plane == 2 ? d.ny : d.nx;
+  const size_t per = (size_t)na * nb;
+  float* dout = nullptr;
+  G3M3_CUDA(m->ctx, cudaMalloc(&dout, 32 * per * sizeof(float)));
+  // J, total B, |B|, E of the box as the step computes them (calcur, fnd_evel, BandE)
+  fields_stage(m, C, box);
+  auto cut = [&](std::initializer_list<const float*> src, int q0) {
+    CutArgs a{};
+    int n = 0;
+    for (const float* p : src) a.src[n++] = p;
+    a.nq = n; a.q0 = q0; a.plane = plane; a.index = index; a.d = d; a.out = dout;
+    launch_cut(a, S(m));
+  };
+  cut({m->bs[0], m->bs[1], m->bs[2], m->btot, m->efld[0], m->efld[1], m->efld[2], m->curr[0], m->curr[1],
+       m->curr[2]}, 0);
+  // per species: velocity with the density floor, pressure parallel /
+  // perpendicular / cross (fnd_pres), density
+  for (int sp = 0; sp < 3; sp++) {
+    const float* pm[3] = {C(m, 10 * sp + 1, box), C(m, 10 * sp + 2, box), C(m, 10 * sp + 3, box)};
+    float* v[3] = {m->vt[0], m->vt[1], m->vt[2]};
+    launch_velocity_floor(C(m, 10 * sp, box), pm, v, m->p.smallbit, m->n3, S(m));
+    const float* pr[3] = {C(m, 10 * sp + 4, box), C(m, 10 * sp + 5, box), C(m, 10 * sp + 6, box)};
+    const float* vv[3] = {m->vt[0], m->vt[1], m->vt[2]};
+    const float* bt[3] = {m->bs[0], m->bs[1], m->bs[2]};
+    launch_fnd_pres(pr, m->ev[0], m->ev[1], m->ev[2], vv, bt, d, S(m));
+    cut({m->vt[0], m->vt[1], m->vt[2], m->ev[0], m->ev[1], m->ev[2], C(m, 10 * sp, box)}, 10 + 7 * sp);
+  }
+  cut({C(m, G3M3_F_EPRES, box)}, 31);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, 32 * per * sizeof(float), cudaMemcpyDeviceToHost, S(m));
+  if (e == cudaSuccess) e = cudaStreamSynchronize(S(m));
+  cudaFree(dout);
+  return e == cudaSuccess ? G3M3_OK : cuda_check(m->ctx, e, "graphing");
+}
+
 int g3m3_model_init_state(g3m3_model* m, float alf_inner, unsigned long long seed, float noise, float iono_lo,
                           float iono_hi) {
   if (!m || noise < 0.0f || !(iono_lo > 0.0f) || iono_hi < iono_lo) return G3M3_ERR_ARG;

@@ -1,4 +1,6 @@
-// k_diag.cu -- flux_counter (sub_flux_counter.f90:5-158): the momentum of
+// k_diag.cu -- diagnostics on the device.
+//
+// flux_counter (sub_flux_counter.f90:5-158): the momentum of
 // each ion species summed over the six walls one cell inside the box faces
 // (index 2 and n-1), counted as inflow or outflow by the sign of the
 // ionospheric-H+ sum, and scaled by grid_spacing / mass.
@@ -7,6 +9,9 @@
 // order, so each of the 18 sums (3 walls x 2 sides x 3 species) is one
 // thread adding in the reference's order (loads issued eight ahead), and
 // one thread then combines them exactly as the reference does.
+//
+// Graphing planes (sub_write_graphing_data.f90:340-420): species velocity
+// with a density floor, and the gather of one grid plane of many arrays.
 #include "kargs.cuh"
 #include "launch.cuh"
 
@@ -82,8 +87,51 @@ __global__ void __launch_bounds__(32) k_flux_counter(const __grid_constant__ Flu
   }
 }
 
+// v = p / max(rho, floor) (sub_write_graphing_data.f90:376-378)
+__global__ void __launch_bounds__(256) k_velocity_floor(const float* __restrict__ rho, const float* __restrict__ px,
+                                                        const float* __restrict__ py, const float* __restrict__ pz,
+                                                        float* vx, float* vy, float* vz, float floor_, size_t n) {
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    const float r = amax1(__ldg(rho + c), floor_);
+    vx[c] = __ldg(px + c) / r;
+    vy[c] = __ldg(py + c) / r;
+    vz[c] = __ldg(pz + c) / r;
+  }
+}
+
+// one plane of nq box arrays: plane 0 = z index, 1 = y index, 2 = x index;
+// out[q][a][b] with the faster grid axis last
+__global__ void __launch_bounds__(256) k_cut(const __grid_constant__ CutArgs a) {
+  const Dims d = a.d;
+  const int na = a.plane == 0 ? d.ny : d.nz;
+  const int nb = a.plane == 2 ? d.ny : d.nx;
+  const int total = a.nq * na * nb;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    const int q = t / (na * nb), r = t % (na * nb), ia = r / nb, ib = r % nb;
+    int i, j, k;
+    if (a.plane == 0) { i = ib + 1; j = ia + 1; k = a.index; }
+    else if (a.plane == 1) { i = ib + 1; j = a.index; k = ia + 1; }
+    else { i = a.index; j = ib + 1; k = ia + 1; }
+    a.out[(size_t)(a.q0 + q) * na * nb + r] = __ldg(a.src[q] + d.at(i, j, k));
+  }
+}
+
 }  // namespace
 
 void launch_flux_counter(const FluxArgs& a, cudaStream_t s) { k_flux_counter<<<1, 32, 0, s>>>(a); }
+
+void launch_velocity_floor(const float* rho, const float* const p[3], float* const v[3], float floor_, size_t n,
+                           cudaStream_t s) {
+  unsigned b = (unsigned)((n + 255) / 256);
+  if (b > 152 * 8) b = 152 * 8;
+  k_velocity_floor<<<b, 256, 0, s>>>(rho, p[0], p[1], p[2], v[0], v[1], v[2], floor_, n);
+}
+
+void launch_cut(const CutArgs& a, cudaStream_t s) {
+  const int na = a.plane == 0 ? a.d.ny : a.d.nz;
+  const int nb = a.plane == 2 ? a.d.ny : a.d.nx;
+  const int total = a.nq * na * nb;
+  k_cut<<<(total + 255) / 256, 256, 0, s>>>(a);
+}
 
 }  // namespace g3m3

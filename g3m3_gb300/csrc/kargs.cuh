@@ -155,6 +155,14 @@ struct FluxArgs {           // flux_counter
   int n_grids, box, advance;   // advance: this launch moves the counter on
 };
 
+struct CutArgs {            // one grid plane of up to 16 box arrays
+  const float* src[16];
+  int nq, q0;              // arrays, and the first output slot they fill
+  int plane, index;        // 0: k = index (x-y), 1: j = index (x-z), 2: i = index (y-z)
+  Dims d;
+  float* out;              // [slot][a][b]
+};
+
 struct SampleArgs {
   const float* field;      // A(nx,ny,nz,n_grids)
   const float* xyz;        // (3,n)

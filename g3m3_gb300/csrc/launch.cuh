@@ -19,6 +19,9 @@ inline unsigned blocks_for(size_t n, unsigned threads) {
 void launch_flux_counter(const FluxArgs& a, cudaStream_t s);
 void launch_craft(const CraftArgs& a, cudaStream_t s);
 void launch_init(const InitArgs& a, cudaStream_t s);
+void launch_velocity_floor(const float* rho, const float* const p[3], float* const v[3], float floor_, size_t n,
+                           cudaStream_t s);
+void launch_cut(const CutArgs& a, cudaStream_t s);
 void launch_push_ion(const PushIonArgs& a, cudaStream_t s);
 void launch_push_field(const PushFieldArgs& a, cudaStream_t s);
 // k_fields.cu

@@ -415,6 +415,16 @@ int g3m3_model_read_fluid(g3m3_model* m, const char* path, int msrf,
  * recorded. */
 int g3m3_model_record_fluxes(g3m3_model* m, const float* scale, int capacity);
 int g3m3_model_fluxes(g3m3_model* m, float* out, int* nsteps);
+/* Graphing plane (sub_write_graphing_data.f90:340-420) of box `box` from
+ * the current state: plane 0 = the x-y plane k = index, 1 = x-z at
+ * j = index, 2 = y-z at i = index.  out[32][na][nb] (nb the faster grid
+ * axis; x-y: ny x nx, x-z: nz x nx, y-z: nz x ny) holds, in code units:
+ * 0-2 total B (b0 + b), 3 |B| (at least smallbit), 4-6 E (BandE), 7-9 J
+ * (calcur); for species q, h, o in turn (10, 17, 24): velocity x, y, z
+ * (p / max(rho, smallbit)), pressure parallel, perpendicular, cross
+ * (fnd_pres), density; 31 electron pressure. */
+int g3m3_model_graphing(g3m3_model* m, int box, int plane, int index,
+    float* out);
 /* Fresh-start state built on the device (3d_main.f90:1268-1629): dipole
  * background of strength alf_inner (moment along -z when negative),
  * corotating ionospheric plasma, the solar-wind fill from the params'

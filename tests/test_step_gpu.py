@@ -212,3 +212,60 @@ def test_craft_records(graph):
             for fi, fq in enumerate(fields):
                 want = _oracle_sample(states[s_][fq], xyz, p)
                 assert r[4 + fi] == want, (s_, c, fq, r[4 + fi], want)
+
+
+@pytest.mark.parametrize("plane", [0, 1, 2])
+def test_graphing_planes(plane):
+    """The graphing plane of box 1 after a step equals the oracle's calcur,
+    total B, fnd_evel, BandE and fnd_pres of the same state, cut the same
+    way."""
+    from oracle import oracle
+    from g3m3_gb300.api import Context, Model
+    st = make_config("tiny3")
+    p = st.params
+    box = 1
+    index = {0: p.nz // 2 + 1, 1: p.ny // 2 + 1, 2: p.nx // 2 + 1}[plane]
+    na = p.ny if plane == 0 else p.nz
+    nb = p.ny if plane == 2 else p.nx
+    with Context() as ctx:
+        m = Model(ctx, st)
+        m.init_steps()
+        m.run(1)
+        s = m.state()
+        got = np.zeros((32, na, nb), np.float32)
+        ctx.check(ctx.L.g3m3_model_graphing(m.h, box, plane, index, got.ctypes.data))
+        m.close()
+    F = [np.ascontiguousarray(s[q]) for q in range(34)]
+    b0 = [np.ascontiguousarray(st.b0[q]) for q in range(3)]
+    dims = [p.nx, p.ny, p.nz, p.n_grids, box]
+    rx = float(p.xspac[box - 1])
+    box3 = (p.nz, p.ny, p.nx)
+    z = lambda: np.zeros(box3, np.float32)
+    cur = [z(), z(), z()]
+    oracle.call("calcur", F[31], F[32], F[33], *dims, *cur, rx, rx, rx)
+    bs = [z(), z(), z()]
+    btot = z()
+    oracle.call("total_b", F[31], F[32], F[33], *b0, *dims, p.smallbit, *bs, btot)
+    ev, tv = [z(), z(), z()], [z(), z(), z()]
+    sp = []
+    for q in (0, 10, 20):
+        sp += [F[q + 1], F[q + 2], F[q + 3], F[q]]
+    oracle.call("fnd_evel", *sp, *cur, *ev, *tv, *dims, p.rmassq, p.rmassh, p.rmasso, p.reynolds)
+    L = st.lists
+    ef = [z(), z(), z()]
+    oracle.call("bande", *ef, *bs, *cur, *ev, btot, F[30], F[0], F[10], F[20], np.ascontiguousarray(st.resistive),
+                p.resist, p.reynolds, *dims, p.rmassq, p.rmassh, p.rmasso, L["ijmid"], L["nummid"], L["ijzero"],
+                p.mbndry, L["numzero"], L["ijmid"].shape[0], L["ijzero"].shape[0], rx, rx, rx)
+    want = [bs[0], bs[1], bs[2], btot, ef[0], ef[1], ef[2], cur[0], cur[1], cur[2]]
+    for q in (0, 10, 20):
+        r = np.maximum(F[q][box - 1], np.float32(p.smallbit))
+        v = [(F[q + 1 + c][box - 1] / r).astype(np.float32) for c in range(3)]
+        par, perp, cross = (np.zeros_like(F[0]) for _ in range(3))
+        oracle.call("fnd_pres", F[q + 4], F[q + 5], F[q + 6], F[q + 7], F[q + 8], F[q + 9], par, perp, cross,
+                    *[np.ascontiguousarray(x) for x in v], *bs, *dims)
+        want += v + [par[box - 1], perp[box - 1], cross[box - 1], F[q][box - 1]]
+    want.append(F[30][box - 1])
+    for qi, w in enumerate(want):
+        w = w[box - 1] if w.ndim == 4 else w
+        cutw = w[index - 1, :, :] if plane == 0 else (w[:, index - 1, :] if plane == 1 else w[:, :, index - 1])
+        assert_same(got[qi], cutw, f"plane {plane} quantity {qi}")
