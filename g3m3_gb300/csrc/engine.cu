@@ -1355,7 +1355,7 @@ int g3m3_model_fluxes(g3m3_model* m, float* out, int* nsteps) {
 }
 
 int g3m3_model_set_variant(g3m3_model* m, int kernel, int variant) {
-  if (!m || kernel != 1 || variant < 0 || variant > 2) return G3M3_ERR_ARG;
+  if (!m || kernel != 1 || variant < 0 || variant > 3) return G3M3_ERR_ARG;
   if (m->fcs_variant != variant) {
     // captured graphs hold the old launch shape
     for (auto& kv : m->graphs) cudaGraphExecDestroy(kv.second);
@@ -1391,7 +1391,7 @@ int g3m3_model_autotune(g3m3_model* m, int* fcs_variant) {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (e == cudaSuccess) e = cudaEventCreate(&e0);
   if (e == cudaSuccess) e = cudaEventCreate(&e1);
-  for (int v = 0; v <= 2 && e == cudaSuccess; v++) {
+  for (int v = 0; v <= 3 && e == cudaSuccess; v++) {
     fa.variant = v;
     launch_fcsmooth(fa, s);   // warm-up
     cudaEventRecord(e0, s);

@@ -281,8 +281,8 @@ __device__ __forceinline__ f2x face_flux2(const float2* P, const float2* Wp, int
   return limiter2(dw, d1m, d1p, chi);
 }
 
-template <int TY>
-__global__ void __launch_bounds__(TX * TY, 2) k_fcsmooth_pair(const __grid_constant__ FcsArgs a) {
+template <int TY, int MINB>
+__global__ void __launch_bounds__(TX * TY, MINB) k_fcsmooth_pair(const __grid_constant__ FcsArgs a) {
   constexpr int NT = TX * TY;
   constexpr int OX = TX + 6, OY = TY + 6;
   constexpr int PX = TX + 4, PY = TY + 4;
@@ -477,19 +477,21 @@ static void launch_ty(const FcsArgs& a, cudaStream_t s) {
   k_fcsmooth_tiled<TY><<<grd, blk, 0, s>>>(a);
 }
 
-template <int TY>
+template <int TY, int MINB>
 static void launch_pair(const FcsArgs& a, cudaStream_t s) {
   const dim3 blk(TX, TY, 1);
   const dim3 grd((unsigned)((a.d.nx + TX - 1) / TX), (unsigned)((a.d.ny + TY - 1) / TY),
                  (unsigned)((a.nf + 1) / 2));
-  k_fcsmooth_pair<TY><<<grd, blk, 0, s>>>(a);
+  k_fcsmooth_pair<TY, MINB><<<grd, blk, 0, s>>>(a);
 }
 
-// variant 0: 32x8 tiles, 1: 32x16 tiles, 2: 32x8 tiles with two fields per
-// block in packed FP32x2 arithmetic
+// variant 0: 32x8 tiles, 1: 32x16 tiles, 2 and 3: 32x8 tiles with two
+// fields per block in packed FP32x2 arithmetic, registers bounded for 3 or
+// 4 resident blocks per SM
 void launch_fcsmooth_tiled(const FcsArgs& a, cudaStream_t s, int variant) {
   if (variant == 1) launch_ty<16>(a, s);
-  else if (variant == 2) launch_pair<8>(a, s);
+  else if (variant == 2) launch_pair<8, 3>(a, s);
+  else if (variant == 3) launch_pair<8, 4>(a, s);
   else launch_ty<8>(a, s);
 }
 

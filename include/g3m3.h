@@ -451,7 +451,8 @@ int g3m3_model_record_craft(g3m3_model* m, int ncraft, const int* npts,
     const float* traj, int nf, const int* fields, int capacity);
 int g3m3_model_craft_records(g3m3_model* m, float* out, int* nsteps);
 /* Tile shapes.  kernel 1 = fcsmooth: variant 0 = 32x8 tiles, 1 = 32x16,
- * 2 = 32x8 tiles with two fields per block in packed FP32x2 arithmetic.
+ * 2 and 3 = 32x8 tiles with two fields per block in packed FP32x2
+ * arithmetic, registers bounded for 3 or 4 resident blocks per SM.
  * Every variant gives the same bits; only the speed differs.
  * g3m3_model_autotune times each variant on scratch copies of box 1 (the
  * state is not changed), keeps the fastest and reports it; cached step
