@@ -310,8 +310,8 @@ def kernel_table(m, reps=20):
 # DRAM bytes (read + write) per launch from one ncu capture of each kernel
 # on a 121x121x61 box (profiles/*_121x121x61.md)
 NCU_TRAFFIC = {
-    "fcsmooth x34": 243.07e6 + 96.28e6,
-    "push_ion": 73.79e6 + 6.69e6,
+    "fcsmooth x34": 243.07e6 + 95.59e6,
+    "push_ion": 73.73e6 + 6.58e6,
     "set_rho+set_speed_agrd": 100.11e6 + 4.78e6,
     "flanks x34": 82.79e6 + 4.61e6,
 }
