@@ -84,7 +84,7 @@ __device__ __forceinline__ float warp_max(float v) {
   return v;
 }
 
-__global__ void __launch_bounds__(256) k_guards(const __grid_constant__ GuardArgs a) {
+__global__ void __launch_bounds__(256, 4) k_guards(const __grid_constant__ GuardArgs a) {
   const Dims d = a.d;
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
