@@ -373,7 +373,10 @@ def run_reference(args):
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": "cell-updates/s", "n_gpus": ws,
             "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": dt / steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": {"workload": WORKLOAD, "parallelism": "host OpenMP"},
+            "data": "synthetic", "config": {"workload": WORKLOAD, "boxes": st.params.n_grids,
+                                            "box": [st.params.nx, st.params.ny, st.params.nz],
+                                            "cells_per_box": st.params.nx * st.params.ny * st.params.nz,
+                                            "parallelism": f"host OpenMP, {os.cpu_count()} threads"},
             "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": os.cpu_count(), "kind": "port",
                              "sample": sample},
             "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
