@@ -24,12 +24,17 @@ struct InnerArgs {          // bndry_inner on box mbndry
   float xmin, ymin, dx, dy, re_equiv, v_rot;
 };
 
+enum FlanksMode { FLANKS_PLAIN = 0, FLANKS_KEEP = 1, FLANKS_REUSE = 2 };
+
 struct FlanksArgs {         // fine box shell from the time-interpolated coarse box
   float* target[G3M3_NFIELDS];
   const float* curc[G3M3_NFIELDS];
   const float* oldc[G3M3_NFIELDS];
   int nf;
   int fields_per_block;     // set by the launcher
+  int mode;                 // FlanksMode
+  long nshell;              // shell cells (set by the launcher)
+  float* ibuf;              // interpolated values [field][shell cell] (KEEP / REUSE)
   Dims d;
   ScalarRef t1;             // (t_new(mb)-t)/(t_new(mb)-t_old(mb)) rounded to FP32
   float sxmin, symin, szmin, sx, sy, sz;        // fine box

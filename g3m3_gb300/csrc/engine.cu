@@ -57,6 +57,7 @@ struct g3m3_model {
   bool inner_set = false;
   float *efld[3], *curr[3], *bs[3], *btot, *ev[3], *tv[3], *vt[3];
   float* glist = nullptr;
+  float* flank_ibuf = nullptr;       // interpolated flank values of a box-step [field][shell cell]
   size_t gcap = 0;
   unsigned* words = nullptr;         // [0] list count, [1..5] maxima scratch, [8+5b..] per-box maxima
   unsigned* host_words = nullptr;
@@ -238,7 +239,8 @@ void inner_stage(g3m3_model* m, Getter target) {
   m->launches_in_step += 1;
 }
 
-void boundary_stage(g3m3_model* m, Getter target, int b, int slot_t1, Getter inner_target = nullptr) {
+void boundary_stage(g3m3_model* m, Getter target, int b, int slot_t1, Getter inner_target = nullptr,
+                    int flank_mode = FLANKS_PLAIN) {
   const g3m3_params& p = m->p;
   const int ng = p.n_grids;
   if (b == ng) {
@@ -259,6 +261,8 @@ void boundary_stage(g3m3_model* m, Getter target, int b, int slot_t1, Getter inn
       a.oldc[q] = O(m, q, b + 1);
     }
     a.nf = G3M3_NFIELDS;
+    a.mode = flank_mode;
+    a.ibuf = m->flank_ibuf;
     fill_flanks_geometry(a, m->d.nx, m->d.ny, m->d.nz, b, p.grd_xmin, p.grd_xmax, p.grd_ymin, p.grd_ymax,
                          p.grd_zmin, p.grd_zmax);
     a.t1 = sref(m, slot_t1);
@@ -449,8 +453,11 @@ int enqueue_box_step(g3m3_model* m, const Action& act) {
     boundary_stage(m, C, b, -1);
   } else {
     // the reference applies the corrector's flanks to the wrk arrays
-    // (3d_main.f90:2599-2637) and bndry_inner to cur (:2640-2658)
-    boundary_stage(m, W, b, act.s_t1c, C);
+    // (3d_main.f90:2599-2637) and bndry_inner to cur (:2640-2658).  The
+    // coarse box stays fixed through this box-step, so the interpolated
+    // flank values at the corrector's time are kept for the two later
+    // stages, which use the same time weight.
+    boundary_stage(m, W, b, act.s_t1c, C, FLANKS_KEEP);
   }
   if ((st = guard_stage(m, C, b, true, false))) return st;
   // Lapidus smoothing (3d_main.f90:2690-2772)
@@ -488,7 +495,7 @@ int enqueue_box_step(g3m3_model* m, const Action& act) {
   lb.nf = 4; lb.d = m->d; lb.delt = sref(m, act.s_full);
   launch_lap(lb, S(m));
   m->launches_in_step += 5;
-  boundary_stage(m, W, b, act.s_t1c);
+  boundary_stage(m, W, b, act.s_t1c, nullptr, FLANKS_REUSE);
   if ((st = guard_stage(m, W, b, true, false))) return st;
   // flux correction (3d_main.f90:2896-3036)
   FcsArgs fa{};
@@ -501,7 +508,7 @@ int enqueue_box_step(g3m3_model* m, const Action& act) {
   fa.nf = G3M3_NFIELDS; fa.d = m->d; fa.variant = m->fcs_variant;
   launch_fcsmooth(fa, S(m));
   m->launches_in_step += 1;
-  boundary_stage(m, C, b, act.s_t1c);
+  boundary_stage(m, C, b, act.s_t1c, nullptr, FLANKS_REUSE);
   return guard_stage(m, C, b, true, true);
 }
 
@@ -557,6 +564,8 @@ int alloc_model(g3m3_model* m) {
   m->gcap = 3 * n3;
   e = cudaMalloc(&m->glist, m->gcap * 11 * sizeof(float));
   if (e != cudaSuccess) return cuda_check(m->ctx, e, "cudaMalloc(limiter list)");
+  e = cudaMalloc(&m->flank_ibuf, (size_t)G3M3_NFIELDS * shell_count(m->d, 2) * sizeof(float));
+  if (e != cudaSuccess) return cuda_check(m->ctx, e, "cudaMalloc(flank values)");
   const size_t nwords = 8 + 5 * (size_t)G3M3_MAX_GRIDS;
   if ((e = cudaMalloc(&m->words, nwords * sizeof(unsigned))) != cudaSuccess) return cuda_check(m->ctx, e, "words");
   if ((e = cudaMemsetAsync(m->words, 0, nwords * sizeof(unsigned), S(m))) != cudaSuccess)
@@ -700,6 +709,7 @@ int g3m3_model_destroy(g3m3_model* m) {
   for (auto& kv : m->graphs) cudaGraphExecDestroy(kv.second);
   if (m->mem) cudaFree(m->mem);
   if (m->glist) cudaFree(m->glist);
+  if (m->flank_ibuf) cudaFree(m->flank_ibuf);
   if (m->words) cudaFree(m->words);
   if (m->host_words) cudaFreeHost(m->host_words);
   if (m->cg) cudaFree(m->cg);

@@ -226,9 +226,12 @@ __device__ __forceinline__ Axis flank_axis(float smin, float sp, int idx, float 
   return r;
 }
 
+template <int MODE>
 __global__ void __launch_bounds__(256) k_flanks(const __grid_constant__ FlanksArgs a) {
   // one thread per shell cell; the interpolation geometry is shared by all
-  // fields, which the thread then walks (blockIdx.y splits the field list)
+  // fields, which the thread then walks (blockIdx.y splits the field list).
+  // FLANKS_KEEP also stores each interpolated value I in ibuf; FLANKS_REUSE
+  // takes I from there (same coarse data and time weight) and only blends.
   const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
   int is, js, ks;
   const Dims d = a.d;
@@ -250,32 +253,43 @@ __global__ void __launch_bounds__(256) k_flanks(const __grid_constant__ FlanksAr
   const size_t c = d.at(is, js, ks);
   const int f_lo = blockIdx.y * a.fields_per_block;
   const int f_hi = min(a.nf, f_lo + a.fields_per_block);
+  const size_t nshell = (size_t)a.nshell;
   // fields in groups of G: every load of a group is issued before its
   // stores, so the loads of a group overlap one another
   constexpr int G = 3;
   for (int f0 = f_lo; f0 < f_hi; f0 += G) {
-    float wo[G][8], wc[G][8], tw[G];
+    float wo[G][8], wc[G][8], tw[G], Ig[G];
 #pragma unroll
     for (int g = 0; g < G; g++) {
       if (f0 + g >= f_hi) break;
-      const float* __restrict__ oc = a.oldc[f0 + g];
-      const float* __restrict__ cc = a.curc[f0 + g];
+      if constexpr (MODE == FLANKS_REUSE) {
+        Ig[g] = __ldg(a.ibuf + (size_t)(f0 + g) * nshell + t);
+      } else {
+        const float* __restrict__ oc = a.oldc[f0 + g];
+        const float* __restrict__ cc = a.curc[f0 + g];
 #pragma unroll
-      for (int q = 0; q < 8; q++) {
-        wo[g][q] = __ldg(oc + c000 + off[q]);
-        wc[g][q] = __ldg(cc + c000 + off[q]);
+        for (int q = 0; q < 8; q++) {
+          wo[g][q] = __ldg(oc + c000 + off[q]);
+          wc[g][q] = __ldg(cc + c000 + off[q]);
+        }
       }
       tw[g] = a.target[f0 + g][c];
     }
 #pragma unroll
     for (int g = 0; g < G; g++) {
       if (f0 + g >= f_hi) break;
-      float wk[8];
+      float I;
+      if constexpr (MODE == FLANKS_REUSE) {
+        I = Ig[g];
+      } else {
+        float wk[8];
 #pragma unroll
-      for (int q = 0; q < 8; q++) wk[q] = wo[g][q] * t1 + wc[g][q] * t2;
-      float I = wk[0] * wgt[0][0] * wgt[0][1] * wgt[0][2];
+        for (int q = 0; q < 8; q++) wk[q] = wo[g][q] * t1 + wc[g][q] * t2;
+        I = wk[0] * wgt[0][0] * wgt[0][1] * wgt[0][2];
 #pragma unroll
-      for (int q = 1; q < 8; q++) I = I + wk[q] * wgt[q][0] * wgt[q][1] * wgt[q][2];
+        for (int q = 1; q < 8; q++) I = I + wk[q] * wgt[q][0] * wgt[q][1] * wgt[q][2];
+        if constexpr (MODE == FLANKS_KEEP) a.ibuf[(size_t)(f0 + g) * nshell + t] = I;
+      }
       float w = tw[g];
       // panels in the reference's order: bottom, top, front, back, left,
       // right; the inner layer blends half and half, the outer layer takes I
@@ -375,9 +389,13 @@ void launch_bndry_inner(const InnerArgs& a, cudaStream_t s) {
 void launch_flanks(const FlanksArgs& a, cudaStream_t s) {
   const long n = shell_count(a.d, 2);
   FlanksArgs b = a;
+  b.nshell = n;
   b.fields_per_block = 6;   // 34 fields over 6 rows of blocks
   const unsigned fy = (unsigned)((a.nf + b.fields_per_block - 1) / b.fields_per_block);
-  k_flanks<<<dim3((unsigned)((n + 255) / 256), fy), 256, 0, s>>>(b);
+  const dim3 grd((unsigned)((n + 255) / 256), fy);
+  if (a.mode == FLANKS_KEEP) k_flanks<FLANKS_KEEP><<<grd, 256, 0, s>>>(b);
+  else if (a.mode == FLANKS_REUSE) k_flanks<FLANKS_REUSE><<<grd, 256, 0, s>>>(b);
+  else k_flanks<FLANKS_PLAIN><<<grd, 256, 0, s>>>(b);
 }
 
 void launch_corer(const CorerArgs& a, cudaStream_t s) {
