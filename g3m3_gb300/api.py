@@ -288,8 +288,12 @@ class Ensemble:
         for m in self.members:
             m.init_steps()
 
-    def run(self, nsteps: int, graph: bool = True):
-        self.ctx.check(self.L.g3m3_ensemble_run(self.h, nsteps, 1 if graph else 0))
+    def run(self, nsteps: int, graph: bool = True, concurrent: bool = False):
+        """graph: one CUDA graph per main step for all members; concurrent
+        (without graph): every member launched at once on its own stream;
+        neither: members one after another."""
+        mode = 1 if graph else (2 if concurrent else 0)
+        self.ctx.check(self.L.g3m3_ensemble_run(self.h, nsteps, mode))
 
     def stats(self):
         k, g, cu = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()

@@ -40,6 +40,8 @@ struct g3m3_model {
   g3m3_ctx* ctx = nullptr;
   cudaStream_t stream = nullptr;     // the context's stream, or the member's own in an ensemble
   bool own_stream = false;
+  cudaStream_t aux[3] = {};          // side streams for independent kernels of a stage
+  cudaEvent_t fork_ev = nullptr, join_ev[3] = {};
   g3m3_params p{};
   Dims d{};
   size_t n3 = 0, n4 = 0;
@@ -55,6 +57,7 @@ struct g3m3_model {
   int num[3][G3M3_MAX_GRIDS] = {};
   int mlen[3] = {};
   bool inner_set = false;
+  bool inner_in_shell = true;        // an inner-boundary cell lies in the two-cell flank shell
   float *efld[3], *curr[3], *bs[3], *btot, *ev[3], *tv[3], *vt[3];
   float* glist = nullptr;
   float* flank_ibuf = nullptr;       // interpolated flank values of a box-step [field][shell cell]
@@ -110,6 +113,22 @@ int scal_slot(g3m3_model* m, float v) {
 ScalarRef sref(g3m3_model* m, int slot) { return ScalarRef{m->h_scal[slot], m->d_scal + slot}; }
 
 cudaStream_t S(g3m3_model* m) { return m->stream; }
+
+// Independent kernels of a stage run on side streams: fork orders the side
+// streams after the work already queued on the model's stream, join orders
+// the model's stream after the side streams' work.  In a captured step the
+// pairs become parallel branches of the graph.
+void fork_aux(g3m3_model* m) {
+  cudaEventRecord(m->fork_ev, S(m));
+  for (int i = 0; i < 3; i++) cudaStreamWaitEvent(m->aux[i], m->fork_ev, 0);
+}
+
+void join_aux(g3m3_model* m) {
+  for (int i = 0; i < 3; i++) {
+    cudaEventRecord(m->join_ev[i], m->aux[i]);
+    cudaStreamWaitEvent(S(m), m->join_ev[i], 0);
+  }
+}
 
 void fields_stage(g3m3_model* m, Getter src, int b) {
   const float rx = m->p.xspac[b - 1];
@@ -182,6 +201,9 @@ void push_stage(g3m3_model* m, Getter out, Getter src, int b, int slot_dt, bool 
   // cur's boundary must be the start-of-step state (see the file comment);
   // epres always goes to cur, B goes to out
   pa.boundary_from_old = 1;
+  // the field push and the three species write disjoint arrays from the
+  // same inputs: the species run beside it on the side streams
+  fork_aux(m);
   if (!out_is_cur) {
     // predictor: only epres lands in cur; B goes to wrk, whose boundary the
     // reference leaves alone -- run the two pushes separately
@@ -215,12 +237,13 @@ void push_stage(g3m3_model* m, Getter out, Getter src, int b, int slot_dt, bool 
     a.rmass = masses[s]; a.grav = m->p.grav; a.re_equiv = m->p.re_equiv; a.reynolds = m->p.reynolds;
     a.delt = sref(m, slot_dt);
     a.boundary_from_old = out_is_cur ? 1 : 0;
-    launch_push_ion(a, S(m));
+    launch_push_ion(a, m->aux[s]);
     m->launches_in_step += 1;
   }
+  join_aux(m);
 }
 
-void inner_stage(g3m3_model* m, Getter target) {
+void inner_stage(g3m3_model* m, Getter target, cudaStream_t st) {
   const g3m3_params& p = m->p;
   InnerArgs a{};
   const int mb = p.mbndry;   // bndry_inner always works on box mbndry
@@ -235,7 +258,7 @@ void inner_stage(g3m3_model* m, Getter target) {
   a.dy = (p.grd_ymax[mb - 1] - p.grd_ymin[mb - 1]) / ((float)m->d.ny - 1.0f);
   a.xmin = p.grd_xmin[mb - 1]; a.ymin = p.grd_ymin[mb - 1];
   a.re_equiv = p.re_equiv; a.v_rot = p.v_rot;
-  launch_bndry_inner(a, S(m));
+  launch_bndry_inner(a, st);
   m->launches_in_step += 1;
 }
 
@@ -243,6 +266,13 @@ void boundary_stage(g3m3_model* m, Getter target, int b, int slot_t1, Getter inn
                     int flank_mode = FLANKS_PLAIN) {
   const g3m3_params& p = m->p;
   const int ng = p.n_grids;
+  // bndry_inner's cells lie deep inside the box, the flank shell on its
+  // faces: with both, bndry_inner runs beside the flanks on a side stream
+  const bool side = b < ng && b <= p.mbndry && m->inner_set && !m->inner_in_shell;
+  if (side) {
+    fork_aux(m);
+    inner_stage(m, inner_target ? inner_target : target, m->aux[0]);
+  }
   if (b == ng) {
     OuterArgs a{};
     for (int q = 0; q < G3M3_NFIELDS; q++) a.f[q] = target(m, q, b);
@@ -269,7 +299,8 @@ void boundary_stage(g3m3_model* m, Getter target, int b, int slot_t1, Getter inn
     launch_flanks(a, S(m));
   }
   m->launches_in_step += 1;
-  if (b <= p.mbndry && m->inner_set) inner_stage(m, inner_target ? inner_target : target);
+  if (side) join_aux(m);
+  else if (b <= p.mbndry && m->inner_set) inner_stage(m, inner_target ? inner_target : target, S(m));
 }
 
 // set_rho and set_speed_agrd; maxima go to the box's slot when `record`
@@ -460,7 +491,9 @@ int enqueue_box_step(g3m3_model* m, const Action& act) {
     boundary_stage(m, W, b, act.s_t1c, C, FLANKS_KEEP);
   }
   if ((st = guard_stage(m, C, b, true, false))) return st;
-  // Lapidus smoothing (3d_main.f90:2690-2772)
+  // Lapidus smoothing (3d_main.f90:2690-2772): the three species beside
+  // the electron-pressure and B chain, each writing its own wrk arrays
+  fork_aux(m);
   for (int s = 0; s < 3; s++) {
     LapArgs la{};
     for (int f = 0; f < 10; f++) {
@@ -474,7 +507,7 @@ int enqueue_box_step(g3m3_model* m, const Action& act) {
     la.vfloor = p.smallbit;
     la.d = m->d;
     la.delt = sref(m, act.s_full);
-    launch_lap(la, S(m));
+    launch_lap(la, m->aux[s]);
   }
   VtotArgs va{};
   for (int s = 0; s < 3; s++) {
@@ -494,6 +527,7 @@ int enqueue_box_step(g3m3_model* m, const Action& act) {
   }
   lb.nf = 4; lb.d = m->d; lb.delt = sref(m, act.s_full);
   launch_lap(lb, S(m));
+  join_aux(m);
   m->launches_in_step += 5;
   boundary_stage(m, W, b, act.s_t1c, nullptr, FLANKS_REUSE);
   if ((st = guard_stage(m, W, b, true, false))) return st;
@@ -691,6 +725,18 @@ int g3m3_model_create(g3m3_ctx* ctx, const g3m3_params* p, g3m3_model** out) {
   m->ctx = ctx;
   m->stream = ctx->stream;
   m->p = *p;
+  {
+    cudaError_t e = cudaEventCreateWithFlags(&m->fork_ev, cudaEventDisableTiming);
+    for (int i = 0; i < 3 && e == cudaSuccess; i++) {
+      e = cudaStreamCreateWithFlags(&m->aux[i], cudaStreamNonBlocking);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&m->join_ev[i], cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) {
+      const int rc = cuda_check(ctx, e, "model streams");
+      g3m3_model_destroy(m);
+      return rc;
+    }
+  }
   m->d = Dims{p->nx, p->ny, p->nz};
   m->n3 = m->d.cells();
   m->n4 = m->n3 * p->n_grids;
@@ -726,6 +772,11 @@ int g3m3_model_destroy(g3m3_model* m) {
   if (m->craft_start) cudaFree(m->craft_start);
   if (m->craft_out) cudaFree(m->craft_out);
   if (m->craft_count) cudaFree(m->craft_count);
+  for (int i = 0; i < 3; i++) {
+    if (m->aux[i]) cudaStreamDestroy(m->aux[i]);
+    if (m->join_ev[i]) cudaEventDestroy(m->join_ev[i]);
+  }
+  if (m->fork_ev) cudaEventDestroy(m->fork_ev);
   if (m->own_stream) cudaStreamDestroy(m->stream);
   delete m;
   return G3M3_OK;
@@ -820,6 +871,15 @@ int g3m3_model_set_inner(g3m3_model* m, const float* resistive, const int* ijsrf
         cudaSuccess)
       return cuda_check(m->ctx, e, "parms");
     m->h_ij[l].assign(ij[l], ij[l] + (size_t)mb * 3 * ml[l]);
+    if (l == 0) m->inner_in_shell = false;
+    for (int b = 0; b < mb; b++)
+      for (int n = 0; n < num[l][b]; n++) {
+        const int i = ij[l][b + (size_t)mb * (0 + 3 * (size_t)n)];
+        const int j = ij[l][b + (size_t)mb * (1 + 3 * (size_t)n)];
+        const int k = ij[l][b + (size_t)mb * (2 + 3 * (size_t)n)];
+        if (i <= 2 || j <= 2 || k <= 2 || i >= m->d.nx - 1 || j >= m->d.ny - 1 || k >= m->d.nz - 1)
+          m->inner_in_shell = true;
+      }
     m->h_parm[l].resize((size_t)mb * 7 * ml[l]);
     if ((e = cudaMemcpy(m->h_parm[l].data(), parm[l], m->h_parm[l].size() * sizeof(float), cudaMemcpyDefault)) !=
         cudaSuccess)
@@ -1512,7 +1572,11 @@ int g3m3_ensemble_member(g3m3_ensemble* e, int i, g3m3_model** out) {
 void* g3m3_ensemble_stream(g3m3_ensemble* e) { return e ? (void*)e->ctx->stream : nullptr; }
 
 int g3m3_ensemble_run(g3m3_ensemble* e, int nsteps, int use_graph) {
-  if (!e || nsteps < 0) return G3M3_ERR_ARG;
+  if (!e || nsteps < 0 || use_graph < 0 || use_graph > 2) return G3M3_ERR_ARG;
+  // 0: members one after another; 1: one graph per main step; 2: every
+  // member launched from the host on its own stream, all at once
+  const bool concurrent = use_graph == 2;
+  if (use_graph == 2) use_graph = 0;
   const size_t nm = e->members.size();
   cudaStream_t origin = e->ctx->stream;
   e->kernels = 0;
@@ -1542,7 +1606,7 @@ int g3m3_ensemble_run(g3m3_ensemble* e, int nsteps, int use_graph) {
         nk += m->launches_in_step;
         if ((ce = cudaEventRecord(e->done[i], S(m))) != cudaSuccess) return cuda_check(e->ctx, ce, "join");
         if ((ce = cudaStreamWaitEvent(origin, e->done[i], 0)) != cudaSuccess) return cuda_check(e->ctx, ce, "join");
-        if (!capture_mode) {
+        if (!capture_mode && !concurrent) {
           // plain mode: one member at a time, launched from the host loop
           if ((ce = cudaStreamSynchronize(S(m))) != cudaSuccess) return cuda_check(e->ctx, ce, "member step");
         }

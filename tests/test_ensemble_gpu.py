@@ -1,6 +1,7 @@
 """Ensembles: members of different box sizes and upstream conditions
-advanced together (one CUDA graph per main step, or one member at a time
-from the host loop) give, member by member, the oracle's bits."""
+advanced together (one CUDA graph per main step, one member at a time from
+the host loop, or all members at once on their own streams) give, member by
+member, the oracle's bits."""
 import numpy as np
 import pytest
 
@@ -16,8 +17,8 @@ def _members(n=3):
     return [ensemble_member(i, n_grids=2, limits=LIMITS) for i in range(n)]
 
 
-@pytest.mark.parametrize("graph", [True, False])
-def test_ensemble_matches_oracle(graph):
+@pytest.mark.parametrize("mode", ["graph", "sequential", "streams"])
+def test_ensemble_matches_oracle(mode):
     from g3m3_gb300.api import Context, Ensemble
     from oracle.oracle import OracleModel
     states = _members()
@@ -32,7 +33,8 @@ def test_ensemble_matches_oracle(graph):
     with Context() as ctx:
         ens = Ensemble(ctx, states)
         ens.init_steps()
-        ens.run(nsteps, graph=graph)
+        graph = mode == "graph"
+        ens.run(nsteps, graph=graph, concurrent=mode == "streams")
         k, g, cu = ens.stats()
         outs = [m.state() for m in ens.members]
         times = [m.times() for m in ens.members]
