@@ -142,14 +142,20 @@ int run_cg(g3m3_ctx* c, const DivbArgs& a, float errlim, bool given, int redos0,
   if (given) divb_launch_init_given(a, s);
   else divb_launch_init(a, s);
   int status = CG_RUNNING;
-  int chunk = 8;
+  // iterations run in chunks between polls of the device-held status; the
+  // first chunk is the previous solve's iteration count on this context
+  // (solves of one run converge alike), the later ones grow from 2, so few
+  // iterations are launched past convergence
+  int chunk = c->cg_hint > 0 ? c->cg_hint : 8;
+  bool first = true;
   for (;;) {
     divb_launch_iterations(a, chunk, s);
     G3M3_CUDA(c, cudaMemcpyAsync(host_st, a.st, sizeof(CgState), cudaMemcpyDeviceToHost, s));
     G3M3_CUDA(c, cudaStreamSynchronize(s));
     status = host_st->status;
     if (status == CG_RUNNING) {
-      if (chunk < 64) chunk *= 2;
+      chunk = first ? 2 : (chunk < 64 ? 2 * chunk : 64);
+      first = false;
       continue;
     }
     if (status == CG_RESTART) {
@@ -171,6 +177,7 @@ int run_cg(g3m3_ctx* c, const DivbArgs& a, float errlim, bool given, int redos0,
     break;
   }
   if (iters_out) *iters_out = host_st->iters;
+  if (status == CG_CONVERGED && host_st->iters > 0 && host_st->iters <= 4096) c->cg_hint = host_st->iters;
   if (residual2_out) *residual2_out = (float)host_st->r2_last;
   if (status_out) *status_out = status;
   G3M3_CUDA(c, cudaGetLastError());

@@ -23,6 +23,7 @@ struct g3m3_ctx {
   // scratch for the drop-in routines, grown on demand
   float* guard_list = nullptr;
   size_t guard_cap = 0;    // entries
+  int cg_hint = 0;                    // iterations of the last converged CG solve
   unsigned* words = nullptr;          // [0] list count, [1..5] maxima
   unsigned* host_words = nullptr;     // pinned
   g3m3::CgState* cg = nullptr;

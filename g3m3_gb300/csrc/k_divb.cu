@@ -214,6 +214,11 @@ __global__ void k_cg_control(DivbArgs a) {
     s->status = CG_CONVERGED;
   } else if (r2 > s->rsq) {
     s->status = CG_RESTART;            // the host restores x and restarts
+  } else if (r2 != r2) {
+    // a NaN residual (an exactly divergence-free B makes the step 0/0) never
+    // passes a test again: the reference iterates to 10*npts with x already
+    // NaN; stop now with the same result and the same not-converged status
+    s->status = CG_MAXIT;
   } else if (s->iters >= s->maxit) {
     s->status = CG_MAXIT;
   } else {
