@@ -230,7 +230,10 @@ def run_ours(args):
                    "parallelism": f"replicas x{ws}",
                    "autotuned": {"fcsmooth": {0: "32x8 tiles", 1: "32x16 tiles",
                                               2: "32x8 tiles, two fields per block, FP32x2, 3 blocks/SM",
-                                              3: "32x8 tiles, two fields per block, FP32x2, 4 blocks/SM"}[fcs_variant]}},
+                                              3: "32x8 tiles, two fields per block, FP32x2, 4 blocks/SM",
+                                              4: "32x8 tiles, two fields per block, FP32x2, cp.async planes, one barrier per plane, 80 registers",
+                                              5: "32x8 tiles, two fields per block, FP32x2, cp.async planes, one barrier per plane, registers unbounded",
+                                              }[fcs_variant]}},
         "other_mode": {"value": cu_p / (ms_p / 1e3), "ms_per_step": ms_p / args.steps,
                        "mode": mode_name[not use_graph]},
         "mode_trial": {"graph": trial[True] * 1e3, "streams": trial[False] * 1e3, "unit": "cell-updates/s",

@@ -1425,7 +1425,8 @@ int g3m3_model_fluxes(g3m3_model* m, float* out, int* nsteps) {
 }
 
 int g3m3_model_set_variant(g3m3_model* m, int kernel, int variant) {
-  if (!m || kernel != 1 || variant < 0 || variant > 3) return G3M3_ERR_ARG;
+  if (!m || kernel != 1 || variant < 0 || variant >= G3M3_FCS_VARIANTS) return G3M3_ERR_ARG;
+  G3M3_CUDA(m->ctx, prepare_fcsmooth());
   if (m->fcs_variant != variant) {
     // captured graphs hold the old launch shape
     for (auto& kv : m->graphs) cudaGraphExecDestroy(kv.second);
@@ -1456,12 +1457,13 @@ int g3m3_model_autotune(g3m3_model* m, int* fcs_variant) {
     fa.chi[q] = q >= G3M3_F_BX ? m->p.diferg : m->p.difrho;
   }
   fa.nf = G3M3_NFIELDS; fa.d = m->d;
+  if (e == cudaSuccess) e = prepare_fcsmooth();
   float best_ms = 0.0f;
   int best = 0;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (e == cudaSuccess) e = cudaEventCreate(&e0);
   if (e == cudaSuccess) e = cudaEventCreate(&e1);
-  for (int v = 0; v <= 3 && e == cudaSuccess; v++) {
+  for (int v = 0; v < G3M3_FCS_VARIANTS && e == cudaSuccess; v++) {
     fa.variant = v;
     launch_fcsmooth(fa, s);   // warm-up
     cudaEventRecord(e0, s);

@@ -18,6 +18,8 @@
 // bytes per cell per field).  The arithmetic is the reference's, operation
 // for operation, including its end rules (copied end differences and end
 // fluxes).
+#include <type_traits>
+
 #include "kargs.cuh"
 #include "launch.cuh"
 
@@ -468,6 +470,275 @@ __global__ void __launch_bounds__(TX * TY, MINB) k_fcsmooth_pair(const __grid_co
   }
 }
 
+__device__ __forceinline__ void st2(float2* p, f2x v) {
+  float lo, hi;
+  upk(v, lo, hi);
+  *p = make_float2(lo, hi);
+}
+
+// face flux with the end rule decided by the caller (inner = m+1 <= n-1)
+__device__ __forceinline__ f2x face_flux2i(const float2* P, const float2* Wp, int o, int st, bool inner, f2x chi) {
+  const f2x dw = sub2(ld2(Wp + o + st), ld2(Wp + o));
+  const f2x d1m = sub2(ld2(P + o), ld2(P + o - st));
+  const f2x d1p = inner ? sub2(ld2(P + o + 2 * st), ld2(P + o + st)) : sub2(ld2(P + o + st), ld2(P + o));
+  return limiter2(dw, d1m, d1p, chi);
+}
+
+// ---- two fields per block, planes copied asynchronously ---------------
+// The pair form above, arranged so the march neither waits for a global
+// load round trip every plane nor spends its instructions on addresses:
+//  * global reads are asynchronous copies into shared memory (cp.async, 4
+//    bytes per field and cell, no register staging) issued two plane steps
+//    ahead of their first reader: step kf issues old kf+3 and wrk kf+2 as one
+//    copy group and, before its barrier, waits for the group of step kf-1
+//    (old kf+2, wrk kf+1), which step kf+1's P1 reads;
+//  * one barrier per plane: P1 and the edge fluxes have four slots each
+//    (plane mod 4, fixed at compile time, the march being unrolled over the
+//    four phases), old and wrk six (plane mod 6, rotated at run time), so no
+//    slot is written in the barrier interval in which another step reads
+//    it, and a copy into a slot starts at least one barrier after the last
+//    read of the plane it held (old kf-3: P1(kf-2); wrk kf-4: the output of
+//    plane kf-5, before step kf-2's barrier);
+//  * shared-memory offsets and edge tests are per-thread constants computed
+//    before the march; halo cells outside the box are zeroed once in every
+//    slot and never copied; the output takes P1(k) and wrk(k) of its own
+//    cell from the register windows.
+// The arithmetic is the pair form's, operation for operation.
+// (The global planes cannot be staged by TMA tensor copies: a row of nx =
+// 121 floats is 484 bytes, and tensor strides must be multiples of 16.)
+__device__ __forceinline__ void cp_async4(uint32_t dst, const float* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+template <int TY>
+struct PcLayout {
+  static constexpr int NT = TX * TY;
+  static constexpr int OX = TX + 6, OY = TY + 6;
+  static constexpr int PX = TX + 4, PY = TY + 4;
+  static constexpr int NO = OX * OY, NP = PX * PY;
+  static constexpr int RO = (NO + NT - 1) / NT, RP = (NP + NT - 1) / NT;
+  static constexpr int NS = 6;                               // old / wrk ring slots
+  static constexpr int O_OFF = 0;                            // float2 offsets
+  static constexpr int W_OFF = O_OFF + NS * NO;
+  static constexpr int P_OFF = W_OFF + NS * NP;
+  static constexpr int FY_OFF = P_OFF + 4 * NP;              // [4][TY+1][TX]
+  static constexpr int FX_OFF = FY_OFF + 4 * (TY + 1) * TX;  // [4][TY]
+  static constexpr size_t BYTES = (size_t)(FX_OFF + 4 * TY) * sizeof(float2);
+};
+
+template <int TY, int MINB>
+__global__ void __launch_bounds__(TX * TY, MINB) k_fcsmooth_pc(const __grid_constant__ FcsArgs a) {
+  using L = PcLayout<TY>;
+  constexpr int NT = L::NT, OX = L::OX, PX = L::PX, NO = L::NO, NP = L::NP, RO = L::RO, RP = L::RP, NS = L::NS;
+  extern __shared__ float2 smem[];
+  float2* const sO = smem + L::O_OFF;
+  float2* const sW = smem + L::W_OFF;
+  float2* const sP = smem + L::P_OFF;
+  float2* const sFy = smem + L::FY_OFF;
+  float2* const sFx = smem + L::FX_OFF;
+  const Dims d = a.d;
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const int f0 = 2 * blockIdx.z;
+  const bool two = f0 + 1 < a.nf;
+  const int f1 = two ? f0 + 1 : f0;
+  const float* __restrict__ W0 = a.wrk[f0];
+  const float* __restrict__ W1 = a.wrk[f1];
+  const float* __restrict__ O0 = a.old[f0];
+  const float* __restrict__ O1 = a.old[f1];
+  float* __restrict__ X0 = a.px[f0];
+  float* __restrict__ X1 = a.px[f1];
+  const f2x chi = pk(a.chi[f0], a.chi[f1]);
+  const f2x six = pk(6.0f, 6.0f);
+  const f2x z2 = pk(0.0f, 0.0f);
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+  const int i0 = blockIdx.x * TX + 1, j0 = blockIdx.y * TY + 1;
+  const int gi = i0 + tx, gj = j0 + ty;
+  const bool mine = gi <= nx && gj <= ny;
+  const size_t plane = (size_t)nx * ny;
+  const uint32_t sO_a = (uint32_t)__cvta_generic_to_shared(sO);
+  const uint32_t sW_a = (uint32_t)__cvta_generic_to_shared(sW);
+
+  int oofs[RO];
+  bool oin[RO];
+#pragma unroll
+  for (int r = 0; r < RO; r++) {
+    const int t = tid + r * NT;
+    const int i = i0 - 3 + t % OX, j = j0 - 3 + t / OX;
+    const bool inbox = i >= 1 && i <= nx && j >= 1 && j <= ny;
+    oin[r] = t < NO && inbox;
+    oofs[r] = (j - 1) * nx + (i - 1);
+    if (t < NO && !inbox) {
+#pragma unroll
+      for (int sl = 0; sl < NS; sl++) sO[sl * NO + t] = make_float2(0.0f, 0.0f);
+    }
+  }
+  int wofs[RP], pO[RP];
+  bool win[RP], pint[RP];
+#pragma unroll
+  for (int r = 0; r < RP; r++) {
+    const int t = tid + r * NT;
+    const int lx = t % PX, ly = t / PX;
+    const int i = i0 - 2 + lx, j = j0 - 2 + ly;
+    const bool inbox = i >= 1 && i <= nx && j >= 1 && j <= ny;
+    win[r] = t < NP && inbox;
+    wofs[r] = (j - 1) * nx + (i - 1);
+    pO[r] = (ly + 1) * OX + lx + 1;
+    pint[r] = !(i == 1 || i == nx || j == 1 || j == ny);
+    if (t < NP && !inbox) {
+#pragma unroll
+      for (int sl = 0; sl < NS; sl++) sW[sl * NP + t] = make_float2(0.0f, 0.0f);
+#pragma unroll
+      for (int sl = 0; sl < 4; sl++) sP[sl * NP + t] = make_float2(0.0f, 0.0f);
+    }
+  }
+  const int cc = (ty + 2) * PX + tx + 2;
+  const bool xin = gi + 1 <= nx - 1, yin = gj + 1 <= ny - 1;
+  const bool xedge = gi == 1 || gi == nx, x2 = gi == 2;
+  const bool yint = gj != 1 && gj != ny, y2 = gj == 2;
+  const int rowoff = (gj - 1) * nx + (gi - 1);
+
+  // asynchronous copies of one plane into a ring slot (both fields of a cell
+  // into the two halves of its float2)
+  auto copy_O = [&](int kp, int slot) {
+    const float* o0 = O0 + (size_t)(kp - 1) * plane;
+    const float* o1 = O1 + (size_t)(kp - 1) * plane;
+    const uint32_t base = sO_a + (uint32_t)(slot * NO + tid) * 8u;
+#pragma unroll
+    for (int r = 0; r < RO; r++)
+      if (oin[r]) {
+        cp_async4(base + r * NT * 8, o0 + oofs[r]);
+        cp_async4(base + r * NT * 8 + 4, o1 + oofs[r]);
+      }
+  };
+  auto copy_W = [&](int kp, int slot) {
+    const float* w0 = W0 + (size_t)(kp - 1) * plane;
+    const float* w1 = W1 + (size_t)(kp - 1) * plane;
+    const uint32_t base = sW_a + (uint32_t)(slot * NP + tid) * 8u;
+#pragma unroll
+    for (int r = 0; r < RP; r++)
+      if (win[r]) {
+        cp_async4(base + r * NT * 8, w0 + wofs[r]);
+        cp_async4(base + r * NT * 8 + 4, w1 + wofs[r]);
+      }
+  };
+
+  // prologue: group 1 = old 1, 2 and wrk 1; group 2 = old 3 and wrk 2 (the
+  // group a step 0 would have issued); wait for group 1
+  copy_O(1, 1);
+  if (2 <= nz) copy_O(2, 2);
+  copy_W(1, 1);
+  cp_async_commit();
+  if (3 <= nz) copy_O(3, 3);
+  if (2 <= nz) copy_W(2, 2);
+  cp_async_commit();
+  cp_async_wait1();
+  __syncthreads();
+
+  f2x p_m1 = z2, p_0 = z2, p_p1 = z2, p_p2 = z2;
+  f2x w_0 = z2, w_p1 = z2;
+  f2x fx_cur = z2, fy_cur = z2, fz_prev = z2;
+  int m6 = 1;   // kf mod 6
+
+  auto step = [&](auto phase, const int kf) {
+    constexpr int PH = decltype(phase)::value;   // kf mod 4: P1 and edge-flux slots
+    constexpr int S0 = PH, S2 = (PH + 2) & 3, S3 = (PH + 3) & 3;
+    const int om = m6 == 0 ? 5 : m6 - 1;            // old kf-1, wrk kf-1
+    const int op = m6 == 5 ? 0 : m6 + 1;            // old kf+1
+    const int o3 = m6 >= 3 ? m6 - 3 : m6 + 3;       // old kf+3
+    const int w2 = m6 >= 4 ? m6 - 4 : m6 + 2;       // wrk kf+2
+    if (kf + 3 <= nz) copy_O(kf + 3, o3);
+    if (kf + 2 <= nz) copy_W(kf + 2, w2);
+    cp_async_commit();
+    if (kf <= nz) {
+      const bool zb = kf == 1 || kf == nz;
+      const float2* Om = sO + om * NO;
+      const float2* Oc = sO + m6 * NO;
+      const float2* Op = sO + op * NO;
+      const float2* Wk = sW + m6 * NP;
+#pragma unroll
+      for (int r = 0; r < RP; r++) {
+        if (win[r]) {
+          const int t = tid + r * NT;
+          const f2x w = ld2(Wk + t);
+          f2x v = w;
+          if (!zb && pint[r]) {
+            const int q = pO[r];
+            const f2x sum = add2(add2(add2(add2(add2(ld2(Oc + q + 1), ld2(Oc + q - 1)), ld2(Oc + q + OX)),
+                                              ld2(Oc + q - OX)),
+                                         ld2(Op + q)),
+                                    ld2(Om + q));
+            v = add2(w, mul2s(chi, sub2(sum, mul2s(six, ld2(Oc + q)))));
+          }
+          st2(sP + S0 * NP + t, v);
+        }
+      }
+    }
+    const int kx = kf - 1;
+    const float2* Wx = sW + om * NP;
+    f2x fx_next = z2, fy_next = z2;
+    if (kx >= 2 && kx <= nz - 1) {
+      const float2* P = sP + S3 * NP;
+      fx_next = face_flux2i(P, Wx, cc, 1, xin, chi);
+      fy_next = face_flux2i(P, Wx, cc, PX, yin, chi);
+      st2(sFy + (S3 * (TY + 1) + ty + 1) * TX + tx, fy_next);
+      if (ty == 0) {
+        st2(sFy + (S3 * (TY + 1)) * TX + tx, face_flux2i(P, Wx, cc - PX, PX, j0 <= ny - 1, chi));
+      } else if (ty == 1 && tx < TY) {
+        st2(sFx + S3 * TY + tx, face_flux2i(P, Wx, (tx + 2) * PX + 1, 1, i0 <= nx - 1, chi));
+      }
+    }
+    cp_async_wait1();   // the group of step kf-1: old kf+2, wrk kf+1
+    __syncthreads();
+    const int k = kf - 2;
+    p_m1 = p_0; p_0 = p_p1; p_p1 = p_p2;
+    p_p2 = (kf <= nz) ? ld2(sP + S0 * NP + cc) : z2;
+    w_0 = w_p1;
+    w_p1 = (kx >= 1 && kx <= nz) ? ld2(Wx + cc) : z2;
+    const f2x fx_left_lane = __shfl_up_sync(0xffffffffu, fx_cur, 1);
+    if (mine && k >= 1) {
+      f2x res;
+      if (k == 1 || k == nz) {
+        res = w_0;
+      } else {
+        f2x tv;
+        if (xedge) {
+          tv = w_0;
+        } else {
+          const f2x fl = x2 ? fx_cur : (tx == 0 ? ld2(sFx + S2 * TY + ty) : fx_left_lane);
+          tv = add2(sub2(p_0, fx_cur), fl);
+        }
+        if (yint) {
+          const f2x fl = y2 ? fy_cur : ld2(sFy + (S2 * (TY + 1) + ty) * TX + tx);
+          tv = add2(sub2(tv, fy_cur), fl);
+        }
+        const f2x d1p_k = (k + 1 <= nz - 1) ? sub2(p_p2, p_p1) : sub2(p_p1, p_0);
+        const f2x fz0 = limiter2(sub2(w_p1, w_0), sub2(p_0, p_m1), d1p_k, chi);
+        const f2x fz1 = k == 2 ? fz0 : fz_prev;
+        fz_prev = fz0;
+        res = add2(sub2(tv, fz0), fz1);
+      }
+      const size_t c = (size_t)(k - 1) * plane + rowoff;
+      float lo, hi;
+      upk(res, lo, hi);
+      X0[c] = lo;
+      if (two) X1[c] = hi;
+    }
+    fx_cur = fx_next;
+    fy_cur = fy_next;
+    m6 = op;
+  };
+  for (int kf = 1; kf <= nz + 2; kf += 4) {
+    step(std::integral_constant<int, 1>{}, kf);
+    if (kf + 1 <= nz + 2) step(std::integral_constant<int, 2>{}, kf + 1);
+    if (kf + 2 <= nz + 2) step(std::integral_constant<int, 3>{}, kf + 2);
+    if (kf + 3 <= nz + 2) step(std::integral_constant<int, 0>{}, kf + 3);
+  }
+  cp_async_wait0();   // no copy outlives the block (all groups past the march are empty)
+}
+
 }  // namespace
 
 template <int TY>
@@ -485,13 +756,41 @@ static void launch_pair(const FcsArgs& a, cudaStream_t s) {
   k_fcsmooth_pair<TY, MINB><<<grd, blk, 0, s>>>(a);
 }
 
+template <int TY, int MINB>
+static cudaError_t prepare_pc() {
+  static cudaError_t done = cudaFuncSetAttribute(k_fcsmooth_pc<TY, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)PcLayout<TY>::BYTES);
+  return done;
+}
+
+template <int TY, int MINB>
+static void launch_pc(const FcsArgs& a, cudaStream_t s) {
+  prepare_pc<TY, MINB>();   // if it failed, the launch below fails and the caller's check reports it
+  const dim3 blk(TX, TY, 1);
+  const dim3 grd((unsigned)((a.d.nx + TX - 1) / TX), (unsigned)((a.d.ny + TY - 1) / TY),
+                 (unsigned)((a.nf + 1) / 2));
+  k_fcsmooth_pc<TY, MINB><<<grd, blk, PcLayout<TY>::BYTES, s>>>(a);
+}
+
+// Dynamic shared-memory limits of the forms that need them, set before any
+// capture (the engine calls this when a variant is chosen).
+cudaError_t prepare_fcsmooth() {
+  cudaError_t e = prepare_pc<8, 3>();
+  if (e == cudaSuccess) e = prepare_pc<8, 2>();
+  return e;
+}
+
 // variant 0: 32x8 tiles, 1: 32x16 tiles, 2 and 3: 32x8 tiles with two
 // fields per block in packed FP32x2 arithmetic, registers bounded for 3 or
-// 4 resident blocks per SM
+// 4 resident blocks per SM; 4 and 5: the two-field form with asynchronous
+// plane copies and one barrier per plane, registers bounded for 3 or 2
+// blocks per SM (shared memory admits 3)
 void launch_fcsmooth_tiled(const FcsArgs& a, cudaStream_t s, int variant) {
   if (variant == 1) launch_ty<16>(a, s);
   else if (variant == 2) launch_pair<8, 3>(a, s);
   else if (variant == 3) launch_pair<8, 4>(a, s);
+  else if (variant == 4) launch_pc<8, 3>(a, s);
+  else if (variant == 5) launch_pc<8, 2>(a, s);
   else launch_ty<8>(a, s);
 }
 

@@ -39,6 +39,7 @@ void launch_total_b(const float* const b[3], const float* const b0[3], float* co
 void launch_lap(const LapArgs& a, cudaStream_t s);
 void launch_vtot(const VtotArgs& a, cudaStream_t s);
 void launch_fcsmooth(const FcsArgs& a, cudaStream_t s);
+cudaError_t prepare_fcsmooth();   // once, outside stream capture
 // k_guards.cu
 void launch_guards(const GuardArgs& a, cudaStream_t s);
 void launch_guard_scatter(const ScatterArgs& a, cudaStream_t s);
