@@ -29,6 +29,156 @@ __device__ __forceinline__ float& S(float* sm, int slot, int f, int ly, int lx) 
   return sm[((slot * NF + f) * HY + ly) * HX + lx];
 }
 
+// Centre-only inputs of one cell.
+struct PushCentre {
+  float old[10], bt, e[3], tv[3];
+};
+
+__device__ __forceinline__ void load_centre(const PushIonArgs& a, size_t c, PushCentre& cin) {
+#pragma unroll
+  for (int f = 0; f < 10; f++) cin.old[f] = __ldg(a.old[f] + c);
+  cin.bt = __ldg(a.btot + c);
+#pragma unroll
+  for (int q = 0; q < 3; q++) cin.e[q] = __ldg(a.efld[q] + c);
+#pragma unroll
+  for (int q = 0; q < 3; q++) cin.tv[q] = __ldg(a.tv[q] + c);
+}
+
+// Scalars of one launch.
+struct PushConst {
+  float delt, dxt, dyt, dzt, rdx, rdy, rdz, bmax, rey, r_bmax, r_rmass;
+};
+
+__device__ __forceinline__ PushConst push_const(const PushIonArgs& a) {
+  PushConst q;
+  q.delt = a.delt.get();
+  q.dxt = 2.0f * a.g.dx; q.dyt = 2.0f * a.g.dy; q.dzt = 2.0f * a.g.dz;
+  q.rdx = 1.0f / q.dxt; q.rdy = 1.0f / q.dyt; q.rdz = 1.0f / q.dzt;
+  q.bmax = 0.20f * a.rmass / q.delt / a.reynolds;
+  q.rey = a.reynolds;
+  q.r_bmax = 1.0f / q.bmax; q.r_rmass = 1.0f / a.rmass;
+  return q;
+}
+
+// The push of one interior cell (sub_push_ion.f90:107-356) from three
+// staged planes [NF][HY][HX] (below, own, above) and the centre-only
+// inputs; the ten results in the reference's field order.
+template <bool POW2>
+__device__ __forceinline__ void push_cell(const float* __restrict__ Plm, const float* __restrict__ Pl0,
+                                          const float* __restrict__ Plp, int tx, int ty, int gi, int gj, int k,
+                                          const PushCentre& cin, const PushIonArgs& a, const PushConst& q,
+                                          float* o) {
+  const float delt = q.delt;
+  const float dxt = q.dxt, dyt = q.dyt, dzt = q.dzt, rdx = q.rdx, rdy = q.rdy, rdz = q.rdz;
+  const float bmax = q.bmax, rey = q.rey, r_bmax = q.r_bmax, r_rmass = q.r_rmass;
+  constexpr float r12 = 1.0f / 12.0f;
+#define DV(a_, d_, rd_) dvd<POW2>((a_), (d_), (rd_))
+  const int ly = ty + 1, lx = tx + 1;
+  // field f at the centre and the six neighbours
+  auto C0 = [&](int f) { return Pl0[(f * HY + ly) * HX + lx]; };
+  auto XP = [&](int f) { return Pl0[(f * HY + ly) * HX + lx + 1]; };
+  auto XM = [&](int f) { return Pl0[(f * HY + ly) * HX + lx - 1]; };
+  auto YP = [&](int f) { return Pl0[(f * HY + ly + 1) * HX + lx]; };
+  auto YM = [&](int f) { return Pl0[(f * HY + ly - 1) * HX + lx]; };
+  auto ZP = [&](int f) { return Plp[(f * HY + ly) * HX + lx]; };
+  auto ZM = [&](int f) { return Plm[(f * HY + ly) * HX + lx]; };
+  auto fluxdiv = [&](int f) -> float {
+    return (DV(XP(f) * XP(VX) - XM(f) * XM(VX), dxt, rdx) + DV(YP(f) * YP(VY) - YM(f) * YM(VY), dyt, rdy))
+           + DV(ZP(f) * ZP(VZ) - ZM(f) * ZM(VZ), dzt, rdz);
+  };
+  const float old0 = cin.old[0], old1 = cin.old[1], old2 = cin.old[2], old3 = cin.old[3], old4 = cin.old[4];
+  const float old5 = cin.old[5], old6 = cin.old[6], old7 = cin.old[7], old8 = cin.old[8], old9 = cin.old[9];
+  const float bt = cin.bt;
+  const float e0 = cin.e[0], e1 = cin.e[1], e2 = cin.e[2];
+  const float tvx = cin.tv[0], tvy = cin.tv[1], tvz = cin.tv[2];
+
+  const float o_rho = old0 - delt * ((DV(XP(1) - XM(1), dxt, rdx) + DV(YP(2) - YM(2), dyt, rdy))
+                                     + DV(ZP(3) - ZM(3), dzt, rdz));
+  const float aqpx = old1 - delt * fluxdiv(1);
+  const float aqpy = old2 - delt * fluxdiv(2);
+  const float aqpz = old3 - delt * fluxdiv(3);
+  float abx = C0(10), aby = C0(11), abz = C0(12);
+  float bmag = bt;
+  const float weight = amax1(1.0f, div_by(bmag, bmax, r_bmax));
+  const float skin_depth = rey / weight;
+  const float tcx = (tvy * abz - tvz * aby);
+  const float tcy = -(tvx * abz - tvz * abx);
+  const float tcz = (tvx * aby - tvy * abx);
+  const float v0x = C0(VX), v0y = C0(VY), v0z = C0(VZ);
+  const float qcx = (v0y * abz - v0z * aby);
+  const float qcy = -(v0x * abz - v0z * abx);
+  const float qcz = (v0x * aby - v0y * abx);
+  const float gpx = DV(XP(4) - XM(4), dxt, rdx) + DV(YP(7) - YM(7), dxt, rdx) + DV(ZP(8) - ZM(8), dxt, rdx);
+  const float gpy = DV(XP(7) - XM(7), dxt, rdx) + DV(YP(5) - YM(5), dyt, rdy) + DV(ZP(9) - ZM(9), dxt, rdx);
+  const float gpz = DV(XP(8) - XM(8), dxt, rdx) + DV(YP(9) - YM(9), dyt, rdy) + DV(ZP(6) - ZM(6), dzt, rdz);
+  const float dex = (e0 + tcx) * rey;
+  const float dey = (e1 + tcy) * rey;
+  const float dez = (e2 + tcz) * rey;
+  const float dvx = (qcx - tcx) * skin_depth;
+  const float dvy = (qcy - tcy) * skin_depth;
+  const float dvz = (qcz - tcz) * skin_depth;
+  const float rho_c = C0(0);
+  const float qden = div_by(rho_c, a.rmass, r_rmass);
+  const float npx = aqpx + delt * (qden * (dex + dvx) - gpx);
+  const float npy = aqpy + delt * (qden * (dey + dvy) - gpy);
+  const float npz = aqpz + delt * (qden * (dez + dvz) - gpz);
+  const float ax = a.g.xmin + a.g.dx * (float)(gi - 1);
+  const float ay = a.g.ymin + a.g.dy * (float)(gj - 1);
+  const float az = a.g.zmin + a.g.dz * (float)(k - 1);
+  const float radius = sqrtf(ax * ax + ay * ay + az * az) + 0.0000001f;
+  const float rr = a.re_equiv * radius;
+  const float g = delt * rho_c * a.grav / (rr * rr);
+  const float r_radius = 1.0f / radius;
+  const float o_px = npx - div_by(g * ax, radius, r_radius);
+  const float o_py = npy - div_by(g * ay, radius, r_radius);
+  const float o_pz = npz - div_by(g * az, radius, r_radius);
+
+  const float wx = C0(4), wy = C0(5), wz = C0(6), wxy = C0(7), wxz = C0(8), wyz = C0(9);
+  const float t2 = 2.0f * delt;
+  const float px_ = old4 - delt * fluxdiv(4) - DV(t2 * wx * (XP(VX) - XM(VX)), dxt, rdx);
+  const float py_ = old5 - delt * fluxdiv(5) - DV(t2 * wy * (YP(VY) - YM(VY)), dyt, rdy);
+  const float pz_ = old6 - delt * fluxdiv(6) - DV(t2 * wz * (ZP(VZ) - ZM(VZ)), dzt, rdz);
+  abx = div_by(6.0f * abx + XP(10) + XM(10) + YP(10) + YM(10) + ZP(10) + ZM(10), 12.0f, r12);
+  aby = div_by(6.0f * aby + XP(11) + XM(11) + YP(11) + YM(11) + ZP(11) + ZM(11), 12.0f, r12);
+  abz = div_by(6.0f * abz + XP(12) + XM(12) + YP(12) + YM(12) + ZP(12) + ZM(12), 12.0f, r12);
+  bmag = sqrtf(abx * abx + aby * aby + abz * abz);
+  float skin = rey;
+  if (bmag > bmax) skin = rey * (bmax / bmag);
+  const float gy2 = div_by(t2 * skin, a.rmass, r_rmass);
+  const float o_xx = px_ - DV(t2 * wxy * (YP(VX) - YM(VX)), dyt, rdy) - DV(t2 * wxz * (ZP(VX) - ZM(VX)), dzt, rdz)
+                     + gy2 * (wxy * abz - wxz * aby);
+  const float o_yy = py_ - DV(t2 * wxy * (XP(VY) - XM(VY)), dxt, rdx) - DV(t2 * wyz * (ZP(VY) - ZM(VY)), dzt, rdz)
+                     + gy2 * (wyz * abx - wxy * abz);
+  const float o_zz = pz_ - DV(t2 * wxz * (XP(VZ) - XM(VZ)), dxt, rdx) - DV(t2 * wyz * (YP(VZ) - YM(VZ)), dyt, rdy)
+                     + gy2 * (wxz * aby - wyz * abx);
+  const float gy1 = div_by(delt * skin, a.rmass, r_rmass);
+  const float o_xy = old7 - delt * fluxdiv(7)
+                     - delt * wxy * (DV(XP(VX) - XM(VX), dxt, rdx) + DV(YP(VY) - YM(VY), dyt, rdy))
+                     - DV(delt * wy * (YP(VX) - YM(VX)), dyt, rdy)
+                     - DV(delt * wx * (XP(VY) - XM(VY)), dxt, rdx)
+                     - DV(delt * wyz * (ZP(VX) - ZM(VX)), dzt, rdz)
+                     - DV(delt * wxz * (ZP(VY) - ZM(VY)), dzt, rdz)
+                     + gy1 * (abz * (wy - wx) - aby * wyz + abx * wxz);
+  const float o_xz = old8 - delt * fluxdiv(8)
+                     - delt * wxz * (DV(XP(VX) - XM(VX), dxt, rdx) + DV(ZP(VZ) - ZM(VZ), dzt, rdz))
+                     - DV(delt * wz * (ZP(VX) - ZM(VX)), dzt, rdz)
+                     - DV(delt * wx * (XP(VZ) - XM(VZ)), dxt, rdx)
+                     - DV(delt * wyz * (YP(VX) - YM(VX)), dyt, rdy)
+                     - DV(delt * wxy * (YP(VZ) - YM(VZ)), dyt, rdy)
+                     + gy1 * (aby * (wx - wz) - abx * wxy + abz * wyz);
+  const float o_yz = old9 - delt * fluxdiv(9)
+                     - delt * wyz * (DV(YP(VY) - YM(VY), dyt, rdy) + DV(ZP(VZ) - ZM(VZ), dzt, rdz))
+                     - DV(delt * wy * (YP(VZ) - YM(VZ)), dyt, rdy)
+                     - DV(delt * wz * (ZP(VY) - ZM(VY)), dzt, rdz)
+                     - DV(delt * wxy * (XP(VZ) - XM(VZ)), dxt, rdx)
+                     - DV(delt * wxz * (XP(VY) - XM(VY)), dxt, rdx)
+                     + gy1 * (abx * (wz - wy) - abz * wxz + aby * wxy);
+  o[0] = o_rho; o[1] = o_px; o[2] = o_py; o[3] = o_pz;
+  o[4] = o_xx; o[5] = o_yy; o[6] = o_zz;
+  o[7] = o_xy; o[8] = o_xz; o[9] = o_yz;
+#undef DV
+}
+
 template <bool POW2>
 __global__ void __launch_bounds__(TX* TY, 3) k_push_ion_tiled(const __grid_constant__ PushIonArgs a, int kchunk) {
   extern __shared__ float sm[];
@@ -88,132 +238,24 @@ __global__ void __launch_bounds__(TX* TY, 3) k_push_ion_tiled(const __grid_const
   if (k_hi == nz - 1) copy_old(nz);
   load_plane(k_lo - 1);
   load_plane(k_lo);
-  const float delt = a.delt.get();
-  const float dxt = 2.0f * a.g.dx, dyt = 2.0f * a.g.dy, dzt = 2.0f * a.g.dz;
-  const float rdx = 1.0f / dxt, rdy = 1.0f / dyt, rdz = 1.0f / dzt;
-  const float bmax = 0.20f * a.rmass / delt / a.reynolds;
-  const float rey = a.reynolds;
-  const float r_bmax = 1.0f / bmax, r_rmass = 1.0f / a.rmass;
-  constexpr float r12 = 1.0f / 12.0f;
-#define DV(a_, d_, rd_) dvd<POW2>((a_), (d_), (rd_))
+  const PushConst q = push_const(a);
   for (int k = k_lo; k <= k_hi; k++) {
     load_plane(k + 1);
     __syncthreads();
     if (mine && !inner_col) {
       copy_old(k);
     } else if (inner_col) {
-      const int sm1 = (k - 1) % 3, s0 = k % 3, sp1 = (k + 1) % 3;
-      const int ly = ty + 1, lx = tx + 1;
-      // field f at the centre and the six neighbours
-      auto C0 = [&](int f) { return S(sm, s0, f, ly, lx); };
-      auto XP = [&](int f) { return S(sm, s0, f, ly, lx + 1); };
-      auto XM = [&](int f) { return S(sm, s0, f, ly, lx - 1); };
-      auto YP = [&](int f) { return S(sm, s0, f, ly + 1, lx); };
-      auto YM = [&](int f) { return S(sm, s0, f, ly - 1, lx); };
-      auto ZP = [&](int f) { return S(sm, sp1, f, ly, lx); };
-      auto ZM = [&](int f) { return S(sm, sm1, f, ly, lx); };
-      auto fluxdiv = [&](int f) -> float {
-        return (DV(XP(f) * XP(VX) - XM(f) * XM(VX), dxt, rdx) + DV(YP(f) * YP(VY) - YM(f) * YM(VY), dyt, rdy))
-               + DV(ZP(f) * ZP(VZ) - ZM(f) * ZM(VZ), dzt, rdz);
-      };
       const size_t c = (size_t)(k - 1) * plane + (size_t)(gj - 1) * nx + (gi - 1);
-      // centre-only inputs
-      const float old0 = __ldg(a.old[0] + c), old1 = __ldg(a.old[1] + c), old2 = __ldg(a.old[2] + c);
-      const float old3 = __ldg(a.old[3] + c), old4 = __ldg(a.old[4] + c), old5 = __ldg(a.old[5] + c);
-      const float old6 = __ldg(a.old[6] + c), old7 = __ldg(a.old[7] + c), old8 = __ldg(a.old[8] + c);
-      const float old9 = __ldg(a.old[9] + c);
-      const float bt = __ldg(a.btot + c);
-      const float e0 = __ldg(a.efld[0] + c), e1 = __ldg(a.efld[1] + c), e2 = __ldg(a.efld[2] + c);
-      const float tvx = __ldg(a.tv[0] + c), tvy = __ldg(a.tv[1] + c), tvz = __ldg(a.tv[2] + c);
-
-      const float o_rho = old0 - delt * ((DV(XP(1) - XM(1), dxt, rdx) + DV(YP(2) - YM(2), dyt, rdy))
-                                         + DV(ZP(3) - ZM(3), dzt, rdz));
-      const float aqpx = old1 - delt * fluxdiv(1);
-      const float aqpy = old2 - delt * fluxdiv(2);
-      const float aqpz = old3 - delt * fluxdiv(3);
-      float abx = C0(10), aby = C0(11), abz = C0(12);
-      float bmag = bt;
-      const float weight = amax1(1.0f, div_by(bmag, bmax, r_bmax));
-      const float skin_depth = rey / weight;
-      const float tcx = (tvy * abz - tvz * aby);
-      const float tcy = -(tvx * abz - tvz * abx);
-      const float tcz = (tvx * aby - tvy * abx);
-      const float v0x = C0(VX), v0y = C0(VY), v0z = C0(VZ);
-      const float qcx = (v0y * abz - v0z * aby);
-      const float qcy = -(v0x * abz - v0z * abx);
-      const float qcz = (v0x * aby - v0y * abx);
-      const float gpx = DV(XP(4) - XM(4), dxt, rdx) + DV(YP(7) - YM(7), dxt, rdx) + DV(ZP(8) - ZM(8), dxt, rdx);
-      const float gpy = DV(XP(7) - XM(7), dxt, rdx) + DV(YP(5) - YM(5), dyt, rdy) + DV(ZP(9) - ZM(9), dxt, rdx);
-      const float gpz = DV(XP(8) - XM(8), dxt, rdx) + DV(YP(9) - YM(9), dyt, rdy) + DV(ZP(6) - ZM(6), dzt, rdz);
-      const float dex = (e0 + tcx) * rey;
-      const float dey = (e1 + tcy) * rey;
-      const float dez = (e2 + tcz) * rey;
-      const float dvx = (qcx - tcx) * skin_depth;
-      const float dvy = (qcy - tcy) * skin_depth;
-      const float dvz = (qcz - tcz) * skin_depth;
-      const float rho_c = C0(0);
-      const float qden = div_by(rho_c, a.rmass, r_rmass);
-      const float npx = aqpx + delt * (qden * (dex + dvx) - gpx);
-      const float npy = aqpy + delt * (qden * (dey + dvy) - gpy);
-      const float npz = aqpz + delt * (qden * (dez + dvz) - gpz);
-      const float ax = a.g.xmin + a.g.dx * (float)(gi - 1);
-      const float ay = a.g.ymin + a.g.dy * (float)(gj - 1);
-      const float az = a.g.zmin + a.g.dz * (float)(k - 1);
-      const float radius = sqrtf(ax * ax + ay * ay + az * az) + 0.0000001f;
-      const float rr = a.re_equiv * radius;
-      const float g = delt * rho_c * a.grav / (rr * rr);
-      const float r_radius = 1.0f / radius;
-      const float o_px = npx - div_by(g * ax, radius, r_radius);
-      const float o_py = npy - div_by(g * ay, radius, r_radius);
-      const float o_pz = npz - div_by(g * az, radius, r_radius);
-
-      const float wx = C0(4), wy = C0(5), wz = C0(6), wxy = C0(7), wxz = C0(8), wyz = C0(9);
-      const float t2 = 2.0f * delt;
-      const float px_ = old4 - delt * fluxdiv(4) - DV(t2 * wx * (XP(VX) - XM(VX)), dxt, rdx);
-      const float py_ = old5 - delt * fluxdiv(5) - DV(t2 * wy * (YP(VY) - YM(VY)), dyt, rdy);
-      const float pz_ = old6 - delt * fluxdiv(6) - DV(t2 * wz * (ZP(VZ) - ZM(VZ)), dzt, rdz);
-      abx = div_by(6.0f * abx + XP(10) + XM(10) + YP(10) + YM(10) + ZP(10) + ZM(10), 12.0f, r12);
-      aby = div_by(6.0f * aby + XP(11) + XM(11) + YP(11) + YM(11) + ZP(11) + ZM(11), 12.0f, r12);
-      abz = div_by(6.0f * abz + XP(12) + XM(12) + YP(12) + YM(12) + ZP(12) + ZM(12), 12.0f, r12);
-      bmag = sqrtf(abx * abx + aby * aby + abz * abz);
-      float skin = rey;
-      if (bmag > bmax) skin = rey * (bmax / bmag);
-      const float gy2 = div_by(t2 * skin, a.rmass, r_rmass);
-      const float o_xx = px_ - DV(t2 * wxy * (YP(VX) - YM(VX)), dyt, rdy) - DV(t2 * wxz * (ZP(VX) - ZM(VX)), dzt, rdz)
-                         + gy2 * (wxy * abz - wxz * aby);
-      const float o_yy = py_ - DV(t2 * wxy * (XP(VY) - XM(VY)), dxt, rdx) - DV(t2 * wyz * (ZP(VY) - ZM(VY)), dzt, rdz)
-                         + gy2 * (wyz * abx - wxy * abz);
-      const float o_zz = pz_ - DV(t2 * wxz * (XP(VZ) - XM(VZ)), dxt, rdx) - DV(t2 * wyz * (YP(VZ) - YM(VZ)), dyt, rdy)
-                         + gy2 * (wxz * aby - wyz * abx);
-      const float gy1 = div_by(delt * skin, a.rmass, r_rmass);
-      const float o_xy = old7 - delt * fluxdiv(7)
-                         - delt * wxy * (DV(XP(VX) - XM(VX), dxt, rdx) + DV(YP(VY) - YM(VY), dyt, rdy))
-                         - DV(delt * wy * (YP(VX) - YM(VX)), dyt, rdy)
-                         - DV(delt * wx * (XP(VY) - XM(VY)), dxt, rdx)
-                         - DV(delt * wyz * (ZP(VX) - ZM(VX)), dzt, rdz)
-                         - DV(delt * wxz * (ZP(VY) - ZM(VY)), dzt, rdz)
-                         + gy1 * (abz * (wy - wx) - aby * wyz + abx * wxz);
-      const float o_xz = old8 - delt * fluxdiv(8)
-                         - delt * wxz * (DV(XP(VX) - XM(VX), dxt, rdx) + DV(ZP(VZ) - ZM(VZ), dzt, rdz))
-                         - DV(delt * wz * (ZP(VX) - ZM(VX)), dzt, rdz)
-                         - DV(delt * wx * (XP(VZ) - XM(VZ)), dxt, rdx)
-                         - DV(delt * wyz * (YP(VX) - YM(VX)), dyt, rdy)
-                         - DV(delt * wxy * (YP(VZ) - YM(VZ)), dyt, rdy)
-                         + gy1 * (aby * (wx - wz) - abx * wxy + abz * wyz);
-      const float o_yz = old9 - delt * fluxdiv(9)
-                         - delt * wyz * (DV(YP(VY) - YM(VY), dyt, rdy) + DV(ZP(VZ) - ZM(VZ), dzt, rdz))
-                         - DV(delt * wy * (YP(VZ) - YM(VZ)), dyt, rdy)
-                         - DV(delt * wz * (ZP(VY) - ZM(VY)), dzt, rdz)
-                         - DV(delt * wxy * (XP(VZ) - XM(VZ)), dxt, rdx)
-                         - DV(delt * wxz * (XP(VY) - XM(VY)), dxt, rdx)
-                         + gy1 * (abx * (wz - wy) - abz * wxz + aby * wxy);
-      a.out[0][c] = o_rho; a.out[1][c] = o_px; a.out[2][c] = o_py; a.out[3][c] = o_pz;
-      a.out[4][c] = o_xx; a.out[5][c] = o_yy; a.out[6][c] = o_zz;
-      a.out[7][c] = o_xy; a.out[8][c] = o_xz; a.out[9][c] = o_yz;
+      PushCentre cin;
+      load_centre(a, c, cin);
+      float o[10];
+      push_cell<POW2>(sm + (size_t)((k - 1) % 3) * NF * HY * HX, sm + (size_t)(k % 3) * NF * HY * HX,
+                      sm + (size_t)((k + 1) % 3) * NF * HY * HX, tx, ty, gi, gj, k, cin, a, q, o);
+#pragma unroll
+      for (int f = 0; f < 10; f++) a.out[f][c] = o[f];
     }
     __syncthreads();
   }
-#undef DV
 }
 
 template <bool POW2>
