@@ -12,16 +12,22 @@ namespace g3m3 {
 namespace {
 
 // Cells of the D-deep outer shell of a box, enumerated as x slabs, then y
-// slabs (x interior), then z slabs (x and y interior).
+// slabs (x interior), then z slabs (x and y interior).  In the x slabs the
+// D cells of one side of a grid row are neighbours in the enumeration
+// (i fastest, then j, then k), so that adjacent threads touch the same
+// 32-byte sectors of the row.
 __device__ __forceinline__ bool shell_cell(long t, int D, const Dims& d, int& i, int& j, int& k) {
   const long nyz = (long)d.ny * d.nz;
   const long xs = 2L * D * nyz;
   if (t < xs) {
-    const int s = (int)(t / nyz);          // 0..2D-1
-    const long r = t % nyz;
-    i = s < D ? s + 1 : d.nx - (2 * D - 1 - s);
-    j = (int)(r % d.ny) + 1;
-    k = (int)(r / d.ny) + 1;
+    const long half = (long)D * nyz;
+    const int side = (int)(t / half);      // 0: i = 1..D, 1: i = nx-D+1..nx
+    const long r = t % half;
+    const int ii = (int)(r % D);
+    const long rr = r / D;
+    i = side == 0 ? ii + 1 : d.nx - D + 1 + ii;
+    j = (int)(rr % d.ny) + 1;
+    k = (int)(rr / d.ny) + 1;
     return true;
   }
   t -= xs;
