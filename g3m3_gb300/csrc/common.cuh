@@ -42,10 +42,8 @@ struct ScalarRef {
 
 __host__ __device__ inline bool is_pow2(float x) {
   if (!(x > 0.0f)) return false;
-  int e = 0;
   // frexp is not available on the device in all modes; use the bits.
   union { float f; uint32_t u; } c{x};
-  (void)e;
   return (c.u & 0x007fffffu) == 0u && ((c.u >> 23) & 0xffu) != 0u && ((c.u >> 23) & 0xffu) != 0xffu;
 }
 

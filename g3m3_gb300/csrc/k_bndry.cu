@@ -396,7 +396,7 @@ void launch_flanks(const FlanksArgs& a, cudaStream_t s) {
   const long n = shell_count(a.d, 2);
   FlanksArgs b = a;
   b.nshell = n;
-  b.fields_per_block = 6;   // 34 fields over 6 rows of blocks
+  b.fields_per_block = 12;   // 34 fields over 3 rows of blocks (12 timed fastest of 3..34 on 121x121x61)
   const unsigned fy = (unsigned)((a.nf + b.fields_per_block - 1) / b.fields_per_block);
   const dim3 grd((unsigned)((n + 255) / 256), fy);
   if (a.mode == FLANKS_KEEP) k_flanks<FLANKS_KEEP><<<grd, 256, 0, s>>>(b);

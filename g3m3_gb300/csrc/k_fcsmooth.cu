@@ -513,25 +513,26 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
-template <int TY>
+template <int TY, int NS_, int NPS_>
 struct PcLayout {
   static constexpr int NT = TX * TY;
   static constexpr int OX = TX + 6, OY = TY + 6;
   static constexpr int PX = TX + 4, PY = TY + 4;
   static constexpr int NO = OX * OY, NP = PX * PY;
   static constexpr int RO = (NO + NT - 1) / NT, RP = (NP + NT - 1) / NT;
-  static constexpr int NS = 6;                               // old / wrk ring slots
+  static constexpr int NS = NS_;                             // old / wrk ring slots
+  static constexpr int NPS = NPS_;                           // P1 ring slots (2 or 4)
   static constexpr int O_OFF = 0;                            // float2 offsets
   static constexpr int W_OFF = O_OFF + NS * NO;
   static constexpr int P_OFF = W_OFF + NS * NP;
-  static constexpr int FY_OFF = P_OFF + 4 * NP;              // [4][TY+1][TX]
+  static constexpr int FY_OFF = P_OFF + NPS * NP;            // [4][TY+1][TX]
   static constexpr int FX_OFF = FY_OFF + 4 * (TY + 1) * TX;  // [4][TY]
   static constexpr size_t BYTES = (size_t)(FX_OFF + 4 * TY) * sizeof(float2);
 };
 
-template <int TY, int MINB>
+template <int TY, int MINB, int NS_, int NPS_>
 __global__ void __launch_bounds__(TX * TY, MINB) k_fcsmooth_pc(const __grid_constant__ FcsArgs a) {
-  using L = PcLayout<TY>;
+  using L = PcLayout<TY, NS_, NPS_>;
   constexpr int NT = L::NT, OX = L::OX, PX = L::PX, NO = L::NO, NP = L::NP, RO = L::RO, RP = L::RP, NS = L::NS;
   extern __shared__ float2 smem[];
   float2* const sO = smem + L::O_OFF;
@@ -591,7 +592,7 @@ __global__ void __launch_bounds__(TX * TY, MINB) k_fcsmooth_pc(const __grid_cons
 #pragma unroll
       for (int sl = 0; sl < NS; sl++) sW[sl * NP + t] = make_float2(0.0f, 0.0f);
 #pragma unroll
-      for (int sl = 0; sl < 4; sl++) sP[sl * NP + t] = make_float2(0.0f, 0.0f);
+      for (int sl = 0; sl < L::NPS; sl++) sP[sl * NP + t] = make_float2(0.0f, 0.0f);
     }
   }
   const int cc = (ty + 2) * PX + tx + 2;
@@ -627,12 +628,12 @@ __global__ void __launch_bounds__(TX * TY, MINB) k_fcsmooth_pc(const __grid_cons
 
   // prologue: group 1 = old 1, 2 and wrk 1; group 2 = old 3 and wrk 2 (the
   // group a step 0 would have issued); wait for group 1
-  copy_O(1, 1);
-  if (2 <= nz) copy_O(2, 2);
-  copy_W(1, 1);
+  copy_O(1, 1 % NS);
+  if (2 <= nz) copy_O(2, 2 % NS);
+  copy_W(1, 1 % NS);
   cp_async_commit();
-  if (3 <= nz) copy_O(3, 3);
-  if (2 <= nz) copy_W(2, 2);
+  if (3 <= nz) copy_O(3, 3 % NS);
+  if (2 <= nz) copy_W(2, 2 % NS);
   cp_async_commit();
   cp_async_wait1();
   __syncthreads();
@@ -640,15 +641,16 @@ __global__ void __launch_bounds__(TX * TY, MINB) k_fcsmooth_pc(const __grid_cons
   f2x p_m1 = z2, p_0 = z2, p_p1 = z2, p_p2 = z2;
   f2x w_0 = z2, w_p1 = z2;
   f2x fx_cur = z2, fy_cur = z2, fz_prev = z2;
-  int m6 = 1;   // kf mod 6
+  int m6 = 1 % NS;   // kf mod NS
 
   auto step = [&](auto phase, const int kf) {
-    constexpr int PH = decltype(phase)::value;   // kf mod 4: P1 and edge-flux slots
-    constexpr int S0 = PH, S2 = (PH + 2) & 3, S3 = (PH + 3) & 3;
-    const int om = m6 == 0 ? 5 : m6 - 1;            // old kf-1, wrk kf-1
-    const int op = m6 == 5 ? 0 : m6 + 1;            // old kf+1
-    const int o3 = m6 >= 3 ? m6 - 3 : m6 + 3;       // old kf+3
-    const int w2 = m6 >= 4 ? m6 - 4 : m6 + 2;       // wrk kf+2
+    constexpr int PH = decltype(phase)::value;   // kf mod 4: edge-flux slots (and P1 slots mod NPS)
+    constexpr int S2 = (PH + 2) & 3, S3 = (PH + 3) & 3;
+    constexpr int P0 = PH % L::NPS, P3 = (PH + 3) % L::NPS;   // P1 of planes kf, kf-1
+    const int om = m6 == 0 ? NS - 1 : m6 - 1;                 // old kf-1, wrk kf-1
+    const int op = m6 == NS - 1 ? 0 : m6 + 1;                 // old kf+1
+    const int o3 = m6 + 3 >= NS ? m6 + 3 - NS : m6 + 3;       // old kf+3
+    const int w2 = m6 + 2 >= NS ? m6 + 2 - NS : m6 + 2;       // wrk kf+2
     if (kf + 3 <= nz) copy_O(kf + 3, o3);
     if (kf + 2 <= nz) copy_W(kf + 2, w2);
     cp_async_commit();
@@ -672,7 +674,7 @@ __global__ void __launch_bounds__(TX * TY, MINB) k_fcsmooth_pc(const __grid_cons
                                     ld2(Om + q));
             v = add2(w, mul2s(chi, sub2(sum, mul2s(six, ld2(Oc + q)))));
           }
-          st2(sP + S0 * NP + t, v);
+          st2(sP + P0 * NP + t, v);
         }
       }
     }
@@ -680,7 +682,7 @@ __global__ void __launch_bounds__(TX * TY, MINB) k_fcsmooth_pc(const __grid_cons
     const float2* Wx = sW + om * NP;
     f2x fx_next = z2, fy_next = z2;
     if (kx >= 2 && kx <= nz - 1) {
-      const float2* P = sP + S3 * NP;
+      const float2* P = sP + P3 * NP;
       fx_next = face_flux2i(P, Wx, cc, 1, xin, chi);
       fy_next = face_flux2i(P, Wx, cc, PX, yin, chi);
       st2(sFy + (S3 * (TY + 1) + ty + 1) * TX + tx, fy_next);
@@ -694,7 +696,7 @@ __global__ void __launch_bounds__(TX * TY, MINB) k_fcsmooth_pc(const __grid_cons
     __syncthreads();
     const int k = kf - 2;
     p_m1 = p_0; p_0 = p_p1; p_p1 = p_p2;
-    p_p2 = (kf <= nz) ? ld2(sP + S0 * NP + cc) : z2;
+    p_p2 = (kf <= nz) ? ld2(sP + P0 * NP + cc) : z2;
     w_0 = w_p1;
     w_p1 = (kx >= 1 && kx <= nz) ? ld2(Wx + cc) : z2;
     const f2x fx_left_lane = __shfl_up_sync(0xffffffffu, fx_cur, 1);
@@ -756,27 +758,29 @@ static void launch_pair(const FcsArgs& a, cudaStream_t s) {
   k_fcsmooth_pair<TY, MINB><<<grd, blk, 0, s>>>(a);
 }
 
-template <int TY, int MINB>
+template <int TY, int MINB, int NS_, int NPS_>
 static cudaError_t prepare_pc() {
-  static cudaError_t done = cudaFuncSetAttribute(k_fcsmooth_pc<TY, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)PcLayout<TY>::BYTES);
+  static cudaError_t done = cudaFuncSetAttribute(k_fcsmooth_pc<TY, MINB, NS_, NPS_>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)PcLayout<TY, NS_, NPS_>::BYTES);
   return done;
 }
 
-template <int TY, int MINB>
+template <int TY, int MINB, int NS_, int NPS_>
 static void launch_pc(const FcsArgs& a, cudaStream_t s) {
-  prepare_pc<TY, MINB>();   // if it failed, the launch below fails and the caller's check reports it
+  prepare_pc<TY, MINB, NS_, NPS_>();   // if it failed, the launch below fails and the caller's check reports it
   const dim3 blk(TX, TY, 1);
   const dim3 grd((unsigned)((a.d.nx + TX - 1) / TX), (unsigned)((a.d.ny + TY - 1) / TY),
                  (unsigned)((a.nf + 1) / 2));
-  k_fcsmooth_pc<TY, MINB><<<grd, blk, PcLayout<TY>::BYTES, s>>>(a);
+  k_fcsmooth_pc<TY, MINB, NS_, NPS_><<<grd, blk, PcLayout<TY, NS_, NPS_>::BYTES, s>>>(a);
 }
 
 // Dynamic shared-memory limits of the forms that need them, set before any
 // capture (the engine calls this when a variant is chosen).
 cudaError_t prepare_fcsmooth() {
-  cudaError_t e = prepare_pc<8, 3>();
-  if (e == cudaSuccess) e = prepare_pc<8, 2>();
+  cudaError_t e = prepare_pc<8, 3, 6, 4>();
+  if (e == cudaSuccess) e = prepare_pc<8, 2, 6, 4>();
+  if (e == cudaSuccess) e = prepare_pc<8, 4, 5, 2>();
   return e;
 }
 
@@ -789,8 +793,9 @@ void launch_fcsmooth_tiled(const FcsArgs& a, cudaStream_t s, int variant) {
   if (variant == 1) launch_ty<16>(a, s);
   else if (variant == 2) launch_pair<8, 3>(a, s);
   else if (variant == 3) launch_pair<8, 4>(a, s);
-  else if (variant == 4) launch_pc<8, 3>(a, s);
-  else if (variant == 5) launch_pc<8, 2>(a, s);
+  else if (variant == 4) launch_pc<8, 3, 6, 4>(a, s);
+  else if (variant == 5) launch_pc<8, 2, 6, 4>(a, s);
+  else if (variant == 6) launch_pc<8, 4, 5, 2>(a, s);
   else launch_ty<8>(a, s);
 }
 

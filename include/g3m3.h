@@ -455,12 +455,13 @@ int g3m3_model_craft_records(g3m3_model* m, float* out, int* nsteps);
  * arithmetic, registers bounded for 3 or 4 resident blocks per SM; 4 and 5
  * = the two-field form with its planes copied asynchronously two plane
  * steps ahead and one barrier per plane (registers bounded for 3 or 2
- * blocks per SM).
+ * blocks per SM); 6 = the same with the shortest rings (5 old/wrk slots,
+ * 2 P1 slots: 55 KB) and 4 blocks per SM.
  * Every variant gives the same bits; only the speed differs.
  * g3m3_model_autotune times each variant on scratch copies of box 1 (the
  * state is not changed), keeps the fastest and reports it; cached step
  * graphs are dropped when the choice changes. */
-#define G3M3_FCS_VARIANTS 6
+#define G3M3_FCS_VARIANTS 7
 int g3m3_model_set_variant(g3m3_model* m, int kernel, int variant);
 int g3m3_model_autotune(g3m3_model* m, int* fcs_variant);
 /* Time bookkeeping: t, t_stepnew(1..n_grids), executed cell-updates. */
