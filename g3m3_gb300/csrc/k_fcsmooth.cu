@@ -492,13 +492,16 @@ __device__ __forceinline__ f2x face_flux2i(const float2* P, const float2* Wp, in
 //    ahead of their first reader: step kf issues old kf+3 and wrk kf+2 as one
 //    copy group and, before its barrier, waits for the group of step kf-1
 //    (old kf+2, wrk kf+1), which step kf+1's P1 reads;
-//  * one barrier per plane: P1 and the edge fluxes have four slots each
-//    (plane mod 4, fixed at compile time, the march being unrolled over the
-//    four phases), old and wrk six (plane mod 6, rotated at run time), so no
-//    slot is written in the barrier interval in which another step reads
-//    it, and a copy into a slot starts at least one barrier after the last
-//    read of the plane it held (old kf-3: P1(kf-2); wrk kf-4: the output of
-//    plane kf-5, before step kf-2's barrier);
+//  * one barrier per plane: the edge fluxes have four slots (plane mod 4,
+//    fixed at compile time, the march being unrolled over the four phases),
+//    P1 four or two (its readers -- the next step's fluxes and this step's
+//    window load after the barrier -- are done one barrier interval after
+//    it is written), old and wrk six or five (plane mod NS, rotated at run
+//    time), so no slot is written in the barrier interval in which another
+//    step reads it, and a copy into a slot starts at least one barrier after
+//    the last read of the plane it held (with five slots: old kf-2, last
+//    read by P1(kf-1); wrk kf-3, last read by the output of plane kf-4
+//    before step kf-1's barrier);
 //  * shared-memory offsets and edge tests are per-thread constants computed
 //    before the march; halo cells outside the box are zeroed once in every
 //    slot and never copied; the output takes P1(k) and wrk(k) of its own
@@ -788,7 +791,8 @@ cudaError_t prepare_fcsmooth() {
 // fields per block in packed FP32x2 arithmetic, registers bounded for 3 or
 // 4 resident blocks per SM; 4 and 5: the two-field form with asynchronous
 // plane copies and one barrier per plane, registers bounded for 3 or 2
-// blocks per SM (shared memory admits 3)
+// blocks per SM (shared memory admits 3); 6: the same with 5-slot old/wrk
+// rings and a 2-slot P1 ring (55 KB), 4 blocks per SM
 void launch_fcsmooth_tiled(const FcsArgs& a, cudaStream_t s, int variant) {
   if (variant == 1) launch_ty<16>(a, s);
   else if (variant == 2) launch_pair<8, 3>(a, s);
