@@ -128,59 +128,85 @@ int ensure_cg_scratch(g3m3_ctx* c, size_t cells) {
 // caller's x and b), iterate in chunks with the control decided on the
 // device, restart after a growing residual (the reference's recursive call,
 // :112-125) until the SAVEd restart count reaches 3.
-int run_cg(g3m3_ctx* c, const DivbArgs& a, float errlim, bool given, int redos0, CgState* host_st,
-           cudaStream_t s, int* iters_out, float* residual2_out, int* status_out) {
-  const size_t n = a.d.cells();
+// One solve as a resumable object: cg_begin queues the initialisation and
+// the first chunk of iterations with a read-back of the status word;
+// cg_step waits for that read-back and queues what the status asks for
+// (the next chunk, a restart, or nothing when the solve has ended), so a
+// caller can keep several solves on separate streams in flight.
+int cg_begin(g3m3_ctx* c, CgRun& r, float errlim, bool given, int redos0, int hint) {
+  const size_t n = r.a.d.cells();
   CgState init{};
   const float e2 = (float)n * (errlim * errlim);   // sub_sparse_solver.f90:53 in FP32
   init.errlim2 = (double)e2;
   init.status = CG_RUNNING;
   init.maxit = (int)((10L * (long)n) > 2000000000L ? 2000000000L : 10L * (long)n);
   init.redos = redos0;
-  *host_st = init;
-  G3M3_CUDA(c, cudaMemcpyAsync(a.st, host_st, sizeof(CgState), cudaMemcpyHostToDevice, s));
-  if (given) divb_launch_init_given(a, s);
-  else divb_launch_init(a, s);
-  int status = CG_RUNNING;
+  *r.host_st = init;
+  G3M3_CUDA(c, cudaMemcpyAsync(r.a.st, r.host_st, sizeof(CgState), cudaMemcpyHostToDevice, r.s));
+  if (given) divb_launch_init_given(r.a, r.s);
+  else divb_launch_init(r.a, r.s);
   // iterations run in chunks between polls of the device-held status; the
-  // first chunk is the previous solve's iteration count on this context
+  // first chunk is the iteration count of an earlier solve of the same kind
   // (solves of one run converge alike), the later ones grow from 2, so few
   // iterations are launched past convergence
-  int chunk = c->cg_hint > 0 ? c->cg_hint : 8;
-  bool first = true;
-  for (;;) {
-    divb_launch_iterations(a, chunk, s);
-    G3M3_CUDA(c, cudaMemcpyAsync(host_st, a.st, sizeof(CgState), cudaMemcpyDeviceToHost, s));
-    G3M3_CUDA(c, cudaStreamSynchronize(s));
-    status = host_st->status;
-    if (status == CG_RUNNING) {
-      chunk = first ? 2 : (chunk < 64 ? 2 * chunk : 64);
-      first = false;
-      continue;
+  r.chunk = hint > 0 ? hint : 8;
+  r.first = true;
+  r.status = CG_RUNNING;
+  divb_launch_iterations(r.a, r.chunk, r.s);
+  G3M3_CUDA(c, cudaMemcpyAsync(r.host_st, r.a.st, sizeof(CgState), cudaMemcpyDeviceToHost, r.s));
+  return G3M3_OK;
+}
+
+int cg_step(g3m3_ctx* c, CgRun& r, bool* done) {
+  *done = false;
+  G3M3_CUDA(c, cudaStreamSynchronize(r.s));
+  r.status = r.host_st->status;
+  if (r.status == CG_RUNNING) {
+    r.chunk = r.first ? 2 : (r.chunk < 64 ? 2 * r.chunk : 64);
+    r.first = false;
+  } else if (r.status == CG_RESTART) {
+    // the residual grew: restore the previous iterate (:118-121); after
+    // three restarts give up (:125), else restart the solver from it
+    if (r.host_st->redos >= 3) {
+      divb_launch_restore(r.a, r.s);
+      r.status = CG_GAVE_UP;
+      *done = true;
+      G3M3_CUDA(c, cudaGetLastError());
+      return G3M3_OK;
     }
-    if (status == CG_RESTART) {
-      // the residual grew: restore the previous iterate (:118-121); after
-      // three restarts give up (:125), else restart the solver from it
-      if (host_st->redos >= 3) {
-        divb_launch_restore(a, s);
-        status = CG_GAVE_UP;
-        break;
-      }
-      CgState& h = *host_st;
-      h.redos += 1;
-      h.status = CG_RUNNING;
-      h.rsq = 0.0; h.anum = 0.0; h.aden = 0.0; h.r2 = 0.0; h.gg = 0.0; h.dgg = 0.0;
-      G3M3_CUDA(c, cudaMemcpyAsync(a.st, host_st, sizeof(CgState), cudaMemcpyHostToDevice, s));
-      divb_launch_restart(a, s);
-      continue;
-    }
-    break;
+    CgState& h = *r.host_st;
+    h.redos += 1;
+    h.status = CG_RUNNING;
+    h.rsq = 0.0; h.anum = 0.0; h.aden = 0.0; h.r2 = 0.0; h.gg = 0.0; h.dgg = 0.0;
+    G3M3_CUDA(c, cudaMemcpyAsync(r.a.st, r.host_st, sizeof(CgState), cudaMemcpyHostToDevice, r.s));
+    divb_launch_restart(r.a, r.s);
+  } else {
+    *done = true;
+    G3M3_CUDA(c, cudaGetLastError());
+    return G3M3_OK;
   }
+  divb_launch_iterations(r.a, r.chunk, r.s);
+  G3M3_CUDA(c, cudaMemcpyAsync(r.host_st, r.a.st, sizeof(CgState), cudaMemcpyDeviceToHost, r.s));
+  return G3M3_OK;
+}
+
+// The CG loop of sparse_solver (sub_sparse_solver.f90:19-159) on a prepared
+// argument block: initialise (from b = div B with x = 0, or from the
+// caller's x and b), iterate in chunks with the control decided on the
+// device, restart after a growing residual (the reference's recursive call,
+// :112-125) until the SAVEd restart count reaches 3.
+int run_cg(g3m3_ctx* c, const DivbArgs& a, float errlim, bool given, int redos0, CgState* host_st,
+           cudaStream_t s, int* iters_out, float* residual2_out, int* status_out) {
+  CgRun r;
+  r.a = a; r.host_st = host_st; r.s = s;
+  int rc = cg_begin(c, r, errlim, given, redos0, c->cg_hint);
+  bool done = false;
+  while (rc == G3M3_OK && !done) rc = cg_step(c, r, &done);
+  if (rc) return rc;
   if (iters_out) *iters_out = host_st->iters;
-  if (status == CG_CONVERGED && host_st->iters > 0 && host_st->iters <= 4096) c->cg_hint = host_st->iters;
+  if (r.status == CG_CONVERGED && host_st->iters > 0 && host_st->iters <= 4096) c->cg_hint = host_st->iters;
   if (residual2_out) *residual2_out = (float)host_st->r2_last;
-  if (status_out) *status_out = status;
-  G3M3_CUDA(c, cudaGetLastError());
+  if (status_out) *status_out = r.status;
   return G3M3_OK;
 }
 

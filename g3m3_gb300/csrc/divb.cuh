@@ -27,6 +27,16 @@ struct DivbArgs {
   int pos[16];
 };
 
+// one CG solve in flight (the host side of cg_begin / cg_step)
+struct CgRun {
+  DivbArgs a;
+  CgState* host_st = nullptr;   // pinned read-back of a.st
+  cudaStream_t s = nullptr;
+  int chunk = 8;
+  bool first = true;
+  int status = 0;
+};
+
 void divb_launch_init(const DivbArgs& a, cudaStream_t s);
 void divb_launch_init_given(const DivbArgs& a, cudaStream_t s);
 void divb_launch_restart(const DivbArgs& a, cudaStream_t s);

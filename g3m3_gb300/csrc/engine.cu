@@ -25,6 +25,8 @@
 namespace g3m3 {
 int run_divb(g3m3_ctx* c, float* bx, float* by, float* bz, const Dims& d, float rx, float errlim, CgState* st,
              CgState* host_st, float* vec, cudaStream_t s, int* iters_out);
+int cg_begin(g3m3_ctx* c, CgRun& r, float errlim, bool given, int redos0, int hint);
+int cg_step(g3m3_ctx* c, CgRun& r, bool* done);
 void fill_flanks_geometry(FlanksArgs& a, int nx, int ny, int nz, int box, const float* gxmin, const float* gxmax,
                           const float* gymin, const float* gymax, const float* gzmin, const float* gzmax);
 void fill_corer_geometry(CorerArgs& a, int nx, int ny, int nz, int box, const float* gxmin, const float* gxmax,
@@ -67,6 +69,14 @@ struct g3m3_model {
   CgState* cg = nullptr;
   CgState* host_cg = nullptr;
   float* cgvec = nullptr;
+  // div B of all boxes at once: per-box solver state, vectors (box 1 uses
+  // cgvec) and streams, made at the first pass
+  CgState* cg_box = nullptr;
+  CgState* host_cg_box = nullptr;
+  float* cgvec_more = nullptr;
+  cudaStream_t divb_stream[G3M3_MAX_GRIDS] = {};
+  cudaEvent_t divb_ev[G3M3_MAX_GRIDS] = {};
+  int cg_hint_box[G3M3_MAX_GRIDS] = {};
   float* d_scal = nullptr;
   float* h_scal = nullptr;
   int nscal = 0, scal_cap = 0;
@@ -760,6 +770,13 @@ int g3m3_model_destroy(g3m3_model* m) {
   if (m->host_words) cudaFreeHost(m->host_words);
   if (m->cg) cudaFree(m->cg);
   if (m->host_cg) cudaFreeHost(m->host_cg);
+  if (m->cg_box) cudaFree(m->cg_box);
+  if (m->host_cg_box) cudaFreeHost(m->host_cg_box);
+  if (m->cgvec_more) cudaFree(m->cgvec_more);
+  for (int b = 0; b < G3M3_MAX_GRIDS; b++) {
+    if (m->divb_stream[b]) cudaStreamDestroy(m->divb_stream[b]);
+    if (m->divb_ev[b]) cudaEventDestroy(m->divb_ev[b]);
+  }
   if (m->d_scal) cudaFree(m->d_scal);
   if (m->h_scal) cudaFreeHost(m->h_scal);
   for (int l = 0; l < 3; l++) {
@@ -931,19 +948,90 @@ int g3m3_model_init_steps(g3m3_model* m) {
   return G3M3_OK;
 }
 
+namespace {
+
+int ensure_divb_boxes(g3m3_model* m) {
+  if (m->cg_box) return G3M3_OK;
+  const int ng = m->p.n_grids;
+  cudaError_t e;
+  if ((e = cudaMalloc(&m->cg_box, ng * sizeof(CgState))) != cudaSuccess) return cuda_check(m->ctx, e, "div B state");
+  if ((e = cudaMallocHost(&m->host_cg_box, ng * sizeof(CgState))) != cudaSuccess)
+    return cuda_check(m->ctx, e, "div B state");
+  if (ng > 1 && (e = cudaMalloc(&m->cgvec_more, (size_t)(ng - 1) * 7 * m->n3 * sizeof(float))) != cudaSuccess)
+    return cuda_check(m->ctx, e, "div B vectors");
+  for (int b = 0; b < ng; b++) {
+    if ((e = cudaStreamCreateWithFlags(&m->divb_stream[b], cudaStreamNonBlocking)) != cudaSuccess)
+      return cuda_check(m->ctx, e, "div B stream");
+    if ((e = cudaEventCreateWithFlags(&m->divb_ev[b], cudaEventDisableTiming)) != cudaSuccess)
+      return cuda_check(m->ctx, e, "div B event");
+  }
+  return G3M3_OK;
+}
+
+}  // namespace
+
+// divB_correct twice per box (3d_main.f90:1067-1096, 3363-3408), then the
+// fine boxes' B copied onto the coarse ones.  A box's solves touch only its
+// own B, so the boxes run side by side, each on its own stream with its own
+// solver state and vectors; every solve is the same sequence of kernels as
+// one run alone.
 int g3m3_model_divb_all(g3m3_model* m) {
   if (!m) return G3M3_ERR_ARG;
   const g3m3_params& p = m->p;
   const int ng = p.n_grids;
+  int st = ensure_divb_boxes(m);
+  if (st) return st;
+  G3M3_CUDA(m->ctx, cudaEventRecord(m->fork_ev, S(m)));
+  CgRun run[G3M3_MAX_GRIDS];
+  int rep[G3M3_MAX_GRIDS] = {};
+  bool fin[G3M3_MAX_GRIDS] = {};
+  for (int b = 1; b <= ng; b++) {
+    CgRun& r = run[b - 1];
+    DivbArgs& a = r.a;
+    a = DivbArgs{};
+    a.bx = C(m, G3M3_F_BX, b); a.by = C(m, G3M3_F_BY, b); a.bz = C(m, G3M3_F_BZ, b);
+    float* vec = b == 1 ? m->cgvec : m->cgvec_more + (size_t)(b - 2) * 7 * m->n3;
+    const size_t n = m->n3;
+    a.rhs = vec; a.x = vec + n; a.xs = vec + 2 * n; a.g = vec + 3 * n; a.h = vec + 4 * n;
+    a.xi = vec + 5 * n; a.xj = vec + 6 * n;
+    a.st = m->cg_box + (b - 1); a.d = m->d;
+    a.rx = a.ry = a.rz = p.xspac[b - 1];
+    r.host_st = m->host_cg_box + (b - 1);
+    r.s = m->divb_stream[b - 1];
+    G3M3_CUDA(m->ctx, cudaStreamWaitEvent(r.s, m->fork_ev, 0));
+  }
+  for (int b = ng; b >= 1; b--) {
+    const int h = m->cg_hint_box[b - 1] > 0 ? m->cg_hint_box[b - 1] : m->ctx->cg_hint;
+    if ((st = cg_begin(m->ctx, run[b - 1], p.divb_errlim, false, 1, h))) return st;
+  }
   int worst = G3M3_OK;
-  for (int b = ng; b >= 1; b--)
-    for (int rep = 0; rep < 2; rep++) {
-      int it = 0;
-      int st = run_divb(m->ctx, C(m, G3M3_F_BX, b), C(m, G3M3_F_BY, b), C(m, G3M3_F_BZ, b), m->d, p.xspac[b - 1],
-                        p.divb_errlim, m->cg, m->host_cg, m->cgvec, S(m), &it);
-      if (st == G3M3_ERR_NOCONV) worst = st;
-      else if (st) return st;
+  for (bool busy = true; busy;) {
+    busy = false;
+    for (int b = ng; b >= 1; b--) {
+      if (fin[b - 1]) continue;
+      busy = true;
+      CgRun& r = run[b - 1];
+      bool done = false;
+      if ((st = cg_step(m->ctx, r, &done))) return st;
+      if (!done) continue;
+      const int iters = r.host_st->iters;
+      if (r.status == CG_CONVERGED && iters > 0 && iters <= 4096) m->cg_hint_box[b - 1] = iters;
+      if (r.status == CG_MAXIT) worst = G3M3_ERR_NOCONV;
+      divb_launch_apply(r.a, r.s);
+      if (rep[b - 1] == 0) {
+        rep[b - 1] = 1;
+        const int h = m->cg_hint_box[b - 1] > 0 ? m->cg_hint_box[b - 1] : m->ctx->cg_hint;
+        if ((st = cg_begin(m->ctx, r, p.divb_errlim, false, 1, h))) return st;
+      } else {
+        fin[b - 1] = true;
+      }
     }
+  }
+  for (int b = 1; b <= ng; b++) {
+    G3M3_CUDA(m->ctx, cudaEventRecord(m->divb_ev[b - 1], run[b - 1].s));
+    G3M3_CUDA(m->ctx, cudaStreamWaitEvent(S(m), m->divb_ev[b - 1], 0));
+  }
+  if (worst) set_err(m->ctx, worst, "div B solver: too many iterations");
   for (int b = ng - 1; b >= 1; b--) {
     SyncedArgs a{};
     for (int q = 0; q < 3; q++) {
