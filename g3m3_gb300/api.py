@@ -231,6 +231,12 @@ class Model:
     def set_state(self, arr):
         self.ctx.check(self.L.g3m3_model_set_state(self.h, addr(arr)))
 
+    def step_host(self, inp, out, graph: bool = False):
+        """One main step from host state ``inp`` to host state ``out`` (the
+        :meth:`state` layout; pinned buffers let the per-box uploads overlap
+        the step)."""
+        self.ctx.check(self.L.g3m3_model_step_host(self.h, addr(inp), addr(out), 1 if graph else 0))
+
     def field(self, which: int, q: int):
         p = self.p
         out = np.empty((p.n_grids, p.nz, p.ny, p.nx), np.float32)

@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cstring>
 #include <map>
+#include <cstdio>
 #include <string>
 #include <vector>
 
@@ -77,6 +78,12 @@ struct g3m3_model {
   cudaStream_t divb_stream[G3M3_MAX_GRIDS] = {};
   cudaEvent_t divb_ev[G3M3_MAX_GRIDS] = {};
   int cg_hint_box[G3M3_MAX_GRIDS] = {};
+  // host-fed step (g3m3_model_step_host): the state to upload while the
+  // next step is enqueued, box by box on a copy stream
+  const float* up_src = nullptr;
+  bool up_waited[G3M3_MAX_GRIDS] = {};
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t up_fork = nullptr, up_ev[G3M3_MAX_GRIDS] = {};
   float* d_scal = nullptr;
   float* h_scal = nullptr;
   int nscal = 0, scal_cap = 0;
@@ -556,9 +563,20 @@ int enqueue_box_step(g3m3_model* m, const Action& act) {
   return guard_stage(m, C, b, true, true);
 }
 
+// the model stream waits for box b's upload before its first use in a
+// host-fed step
+int upload_wait(g3m3_model* m, int b) {
+  if (!m->up_src || b < 1 || b > m->p.n_grids || m->up_waited[b - 1]) return G3M3_OK;
+  G3M3_CUDA(m->ctx, cudaStreamWaitEvent(S(m), m->up_ev[b - 1], 0));
+  m->up_waited[b - 1] = true;
+  return G3M3_OK;
+}
+
 int enqueue_plan(g3m3_model* m, const std::vector<Action>& acts) {
   for (const Action& a : acts) {
     int st = G3M3_OK;
+    // an action reads box a.box and the coarser box a.box+1
+    if ((st = upload_wait(m, a.box)) || (st = upload_wait(m, a.box + 1))) return st;
     switch (a.kind) {
       case Action::BOX_STEP: st = enqueue_box_step(m, a); break;
       case Action::CORE_SYNC: corer_stage(m, a.box); break;
@@ -661,7 +679,23 @@ int step_enqueue(g3m3_model* m, const std::vector<Action>& acts) {
   if ((e = cudaMemcpyAsync(m->d_scal, m->h_scal, m->scal_cap * sizeof(float), cudaMemcpyHostToDevice, S(m))) !=
       cudaSuccess)
     return cuda_check(m->ctx, e, "scalar upload");
+  if (m->up_src) {
+    // host-fed step: each box's current state on the copy stream, coarsest
+    // box first (the order the step first touches them), one event per box
+    const int ng = m->p.n_grids;
+    G3M3_CUDA(m->ctx, cudaEventRecord(m->up_fork, S(m)));
+    G3M3_CUDA(m->ctx, cudaStreamWaitEvent(m->copy_stream, m->up_fork, 0));
+    for (int b = ng; b >= 1; b--) {
+      for (int f = 0; f < G3M3_NFIELDS; f++)
+        G3M3_CUDA(m->ctx, cudaMemcpyAsync(C(m, f, b), m->up_src + (size_t)f * m->n4 + (size_t)(b - 1) * m->n3,
+                                          m->n3 * sizeof(float), cudaMemcpyHostToDevice, m->copy_stream));
+      G3M3_CUDA(m->ctx, cudaEventRecord(m->up_ev[b - 1], m->copy_stream));
+      m->up_waited[b - 1] = false;
+    }
+  }
   if (m->flux_cap > 0) {
+    for (int b = m->p.n_grids; b >= 1; b--)
+      if (int st = upload_wait(m, b)) return st;
     // flux_counter of every box at the start of the main step (3d_main.f90:1997-2011)
     for (int b = m->p.n_grids; b >= 1; b--) {
       FluxArgs fa{};
@@ -678,6 +712,8 @@ int step_enqueue(g3m3_model* m, const std::vector<Action>& acts) {
   }
   int rc = enqueue_plan(m, acts);
   if (rc) return rc;
+  for (int b = 1; b <= m->p.n_grids; b++)   // every upload joins the model stream
+    if ((rc = upload_wait(m, b))) return rc;
   if (m->craft_cap > 0 && m->craft_t_slot >= 0) {
     // virtual spacecraft at the end of the step (cft_craft_handling.f90:120-200)
     CraftArgs ca{};
@@ -776,7 +812,10 @@ int g3m3_model_destroy(g3m3_model* m) {
   for (int b = 0; b < G3M3_MAX_GRIDS; b++) {
     if (m->divb_stream[b]) cudaStreamDestroy(m->divb_stream[b]);
     if (m->divb_ev[b]) cudaEventDestroy(m->divb_ev[b]);
+    if (m->up_ev[b]) cudaEventDestroy(m->up_ev[b]);
   }
+  if (m->copy_stream) cudaStreamDestroy(m->copy_stream);
+  if (m->up_fork) cudaEventDestroy(m->up_fork);
   if (m->d_scal) cudaFree(m->d_scal);
   if (m->h_scal) cudaFreeHost(m->h_scal);
   for (int l = 0; l < 3; l++) {
@@ -1049,53 +1088,104 @@ int g3m3_model_divb_all(g3m3_model* m) {
   return worst;
 }
 
+namespace {
+
+// One main step: plan, enqueue or replay, wait, finish (div B when due).
+int one_step(g3m3_model* m, int use_graph, std::vector<Action>& acts) {
+  cudaStream_t s = S(m);
+  std::string key;
+  int rc = step_plan(m, acts, key);
+  if (rc) return rc;
+  if (m->up_src) {   // the capture holds copies from this host buffer
+    char buf[40];
+    snprintf(buf, sizeof buf, "|up%p", (const void*)m->up_src);
+    key += buf;
+  }
+  cudaError_t e;
+  if (use_graph) {
+    auto found = m->graphs.find(key);
+    if (found == m->graphs.end()) {
+      // capture: scalar upload from the pinned table, the step, and the
+      // read-back of the recorded maxima
+      Roles saved = save_roles(m);
+      cudaGraph_t g = nullptr;
+      if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+        return cuda_check(m->ctx, e, "begin capture");
+      rc = step_enqueue(m, acts);
+      cudaError_t e2 = cudaStreamEndCapture(s, &g);
+      restore_roles(m, saved);   // capture did not run anything
+      if (rc || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        if (rc) return rc;
+        return cuda_check(m->ctx, e2, "graph capture");
+      }
+      cudaGraphExec_t ex = nullptr;
+      e = cudaGraphInstantiate(&ex, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return cuda_check(m->ctx, e, "graph instantiate");
+      found = m->graphs.emplace(key, ex).first;
+      m->kernel_nodes[key] = m->launches_in_step;
+    }
+    if ((e = cudaGraphLaunch(found->second, s)) != cudaSuccess) return cuda_check(m->ctx, e, "graph launch");
+    apply_role_swaps(m, acts);
+    m->graph_launches += 1;
+    m->kernels += m->kernel_nodes[key];
+  } else {
+    if ((rc = step_enqueue(m, acts))) return rc;
+    m->kernels += m->launches_in_step;
+  }
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(m->ctx, e, "main step");
+  return step_finish(m);
+}
+
+int ensure_copy_stream(g3m3_model* m) {
+  if (m->copy_stream) return G3M3_OK;
+  G3M3_CUDA(m->ctx, cudaStreamCreateWithFlags(&m->copy_stream, cudaStreamNonBlocking));
+  G3M3_CUDA(m->ctx, cudaEventCreateWithFlags(&m->up_fork, cudaEventDisableTiming));
+  for (int b = 0; b < m->p.n_grids; b++)
+    G3M3_CUDA(m->ctx, cudaEventCreateWithFlags(&m->up_ev[b], cudaEventDisableTiming));
+  return G3M3_OK;
+}
+
+bool pinned(const void* p) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeHost;
+}
+
+}  // namespace
+
 int g3m3_model_run(g3m3_model* m, int nsteps, int use_graph) {
   if (!m || nsteps < 0) return G3M3_ERR_ARG;
   m->kernels = 0;
   m->graph_launches = 0;
-  cudaStream_t s = S(m);
   std::vector<Action> acts;
-  for (int it = 0; it < nsteps; it++) {
-    std::string key;
-    int rc = step_plan(m, acts, key);
-    if (rc) return rc;
-    cudaError_t e;
-    if (use_graph) {
-      auto found = m->graphs.find(key);
-      if (found == m->graphs.end()) {
-        // capture: scalar upload from the pinned table, the step, and the
-        // read-back of the recorded maxima
-        Roles saved = save_roles(m);
-        cudaGraph_t g = nullptr;
-        if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
-          return cuda_check(m->ctx, e, "begin capture");
-        rc = step_enqueue(m, acts);
-        cudaError_t e2 = cudaStreamEndCapture(s, &g);
-        restore_roles(m, saved);   // capture did not run anything
-        if (rc || e2 != cudaSuccess) {
-          if (g) cudaGraphDestroy(g);
-          if (rc) return rc;
-          return cuda_check(m->ctx, e2, "graph capture");
-        }
-        cudaGraphExec_t ex = nullptr;
-        e = cudaGraphInstantiate(&ex, g, 0);
-        cudaGraphDestroy(g);
-        if (e != cudaSuccess) return cuda_check(m->ctx, e, "graph instantiate");
-        found = m->graphs.emplace(key, ex).first;
-        m->kernel_nodes[key] = m->launches_in_step;
-      }
-      if ((e = cudaGraphLaunch(found->second, s)) != cudaSuccess) return cuda_check(m->ctx, e, "graph launch");
-      apply_role_swaps(m, acts);
-      m->graph_launches += 1;
-      m->kernels += m->kernel_nodes[key];
-    } else {
-      if ((rc = step_enqueue(m, acts))) return rc;
-      m->kernels += m->launches_in_step;
-    }
-    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(m->ctx, e, "main step");
-    if ((rc = step_finish(m))) return rc;
-  }
+  for (int it = 0; it < nsteps; it++)
+    if (int rc = one_step(m, use_graph, acts)) return rc;
   return G3M3_OK;
+}
+
+int g3m3_model_step_host(g3m3_model* m, const float* in, float* out, int use_graph) {
+  if (!m || !in || !out) return G3M3_ERR_ARG;
+  m->kernels = 0;
+  m->graph_launches = 0;
+  if (!pinned(in)) {   // pageable input: plain upload, then the step
+    int rc = g3m3_model_set_state(m, in);
+    if (!rc) rc = g3m3_model_run(m, 1, use_graph);
+    if (!rc) rc = g3m3_model_get_state(m, out);
+    return rc;
+  }
+  int rc = ensure_copy_stream(m);
+  if (rc) return rc;
+  std::vector<Action> acts;
+  m->up_src = in;
+  rc = one_step(m, use_graph, acts);
+  m->up_src = nullptr;
+  if (rc) return rc;
+  return g3m3_model_get_state(m, out);
 }
 
 int g3m3_model_time_kernel(g3m3_model* m, int kernel, int box, int reps, float* ms_per_launch, double* bytes) {

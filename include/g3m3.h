@@ -394,6 +394,17 @@ int g3m3_model_init_steps(g3m3_model* m);
 /* Run nsteps main steps.  use_graph: 0 = launch kernels from the host loop
  * (plain), 1 = replay one captured CUDA graph per main step. */
 int g3m3_model_run(g3m3_model* m, int nsteps, int use_graph);
+/* One main step from host state to host state.  `in` holds the state in
+ * the g3m3_model_set_state layout (34 fields x n_grids x nz x ny x nx
+ * floats); it is uploaded box by box, coarsest first, on a copy stream, and
+ * the step waits for a box's upload only before it first touches that box,
+ * so the finer boxes' uploads overlap the coarser boxes' steps.  After the
+ * step (and the div B pass when one is due) the state is read back into
+ * `out` (the same layout; it may be `in`).  With pinned buffers
+ * (cudaMallocHost / cudaHostAlloc) the copies overlap as described and a
+ * graph captured for a buffer is reused while the buffer stays the same;
+ * pageable buffers are copied in and out around the step. */
+int g3m3_model_step_host(g3m3_model* m, const float* in, float* out, int use_graph);
 /* div B cleaning of every box plus flanks_synced and bndry_corer
  * (3d_main.f90:3363-3408). */
 int g3m3_model_divb_all(g3m3_model* m);

@@ -102,6 +102,37 @@ def test_fcsmooth_variants(cfg, nsteps, variant):
     assert np.array_equal(tsn, om.t_stepnew)
 
 
+@pytest.mark.parametrize("graph,pin", [(False, True), (True, True), (False, False)])
+def test_step_host(graph, pin):
+    """Host-fed main steps (per-box uploads overlapping the step, result
+    read back, fed in again) give the oracle's bits after two steps, with
+    pinned buffers (graph or host launches) and with pageable ones."""
+    import torch
+    from oracle.oracle import OracleModel
+    from g3m3_gb300.api import Context, Model
+    st = make_config("mid3")
+    om = OracleModel(st, omp=True)
+    om.init_steps()
+    for _ in range(2):
+        assert om.main_step() == 0
+    with Context() as ctx:
+        m = Model(ctx, st)
+        m.init_steps()
+        if pin:
+            buf_t = torch.empty(st.cur.shape, dtype=torch.float32, pin_memory=True)
+            buf = buf_t.numpy()
+        else:
+            buf = np.empty(st.cur.shape, np.float32)
+        m.state(out=buf)   # the state init_steps prepared
+        for _ in range(2):
+            m.step_host(buf, buf, graph=graph)
+        tsn = m.times()[1]
+        m.close()
+    for q in range(34):
+        assert_same(buf[q], om.cur[q], f"field {q}")
+    assert np.array_equal(tsn, om.t_stepnew)
+
+
 def test_autotuned_steps():
     """Autotuning picks a tile shape on scratch copies: the state it leaves
     and the steps after it are the oracle's."""
