@@ -575,8 +575,10 @@ int upload_wait(g3m3_model* m, int b) {
 int enqueue_plan(g3m3_model* m, const std::vector<Action>& acts) {
   for (const Action& a : acts) {
     int st = G3M3_OK;
-    // an action reads box a.box and the coarser box a.box+1
+    // an action reads box a.box and the coarser box a.box+1; the box-steps
+    // of boxes up to mbndry also run bndry_inner on box mbndry
     if ((st = upload_wait(m, a.box)) || (st = upload_wait(m, a.box + 1))) return st;
+    if (a.box <= m->p.mbndry && (st = upload_wait(m, m->p.mbndry))) return st;
     switch (a.kind) {
       case Action::BOX_STEP: st = enqueue_box_step(m, a); break;
       case Action::CORE_SYNC: corer_stage(m, a.box); break;
