@@ -88,6 +88,43 @@ def test_divb_all():
         assert_same(g[q], om.cur[q], f"divb untouched field {q}")
 
 
+@pytest.mark.parametrize("host_fed", [False, True])
+def test_divb_inside_steps(host_fed):
+    """Two main steps with div B due after the second (all boxes solved side
+    by side): the fields div B does not touch are the oracle's bits, B is
+    within the CG tolerance of the oracle's cleaning, host-fed (graph) or
+    not."""
+    import torch
+    from oracle.oracle import OracleModel
+    from g3m3_gb300.api import Context, Model
+    st = make_config("mid3", divb_every=2, divb_errlim=1e-5)
+    om = OracleModel(st, omp=True)     # its second main step ends with div B
+    om.init_steps()
+    o0 = OracleModel(make_config("mid3", divb_every=0, divb_errlim=1e-5), omp=True)
+    o0.init_steps()
+    for _ in range(2):
+        assert om.main_step() == 0
+        assert o0.main_step() == 0
+    before = o0.cur
+    with Context() as ctx:
+        m = Model(ctx, st)
+        m.init_steps()
+        if host_fed:
+            buf = torch.empty(st.cur.shape, dtype=torch.float32, pin_memory=True).numpy()
+            m.state(out=buf)
+            for _ in range(2):
+                m.step_host(buf, buf, graph=True)
+            g = buf
+        else:
+            m.run(2, graph=False)
+            g = m.state()
+        m.close()
+    for q in range(31):
+        assert_same(g[q], om.cur[q], f"field {q}")
+    for q in (31, 32, 33):
+        assert rel_l2(g[q] - before[q], om.cur[q] - before[q]) < 0.2
+
+
 @pytest.mark.parametrize("cfg,nsteps,variant", [("tiny3", 2, 1), ("mid3", 2, 1), ("tiny3", 2, 2), ("mid3", 2, 2),
                                                ("mid3", 2, 3), ("tiny3", 2, 4), ("mid3", 2, 4), ("tiny3", 2, 5),
                                                ("mid3", 2, 5), ("tiny3", 2, 6), ("mid3", 2, 6)])
