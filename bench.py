@@ -283,21 +283,24 @@ def run_batched(args, device, members=16):
         e1 = torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         e0.record(stream)
-        ens.run(nsteps, graph=mode == "graph", concurrent=mode == "streams")
+        ens.run(nsteps, graph=mode in ("graph", "member_graphs"), concurrent=mode in ("streams", "member_graphs"))
         e1.record(stream)
         torch.cuda.synchronize()
         k, _, cu1 = ens.stats()
         return e0.elapsed_time(e1), cu1 - cu0, k
 
     ens.run(max(args.warmup, 2), graph=True)   # captures the step graphs
+    ens.run(2, graph=True, concurrent=True)    # and every member's own graphs
     ens.run(1, graph=False, concurrent=True)
     ms_g, cu_g, k_g = timed(args.steps, "graph")
+    ms_m, cu_m, k_m = timed(args.steps, "member_graphs")
     ms_c, cu_c, _ = timed(args.steps, "streams")
     n_p = max(2, args.steps // 2)
     ms_p, cu_p, _ = timed(n_p, "sequential")
     ens.close()
     ctx.close()
     vg, vc, vp = cu_g / (ms_g / 1e3), cu_c / (ms_c / 1e3), cu_p / (ms_p / 1e3)
+    vm = cu_m / (ms_m / 1e3)
     return {"workload": f"ensemble of {members} nested grids, 5 boxes each, box sizes "
                         + ", ".join(f"{a}x{b}x{c}" for a, b, c in cells) + " cycling; upstream n, |v|, IMF "
                         "clock angle and |B| drawn from the seed",
@@ -305,12 +308,15 @@ def run_batched(args, device, members=16):
             "graph": {"value": vg, "unit": "cell-updates/s", "ms_per_step": ms_g / args.steps, "steps": args.steps,
                       "gpu_launches": int(k_g), "mode": "one CUDA graph per main step for all members, "
                       "members on their own streams"},
+            "member_graphs": {"value": vm, "unit": "cell-updates/s", "ms_per_step": ms_m / args.steps,
+                              "steps": args.steps, "gpu_launches": int(k_m),
+                              "mode": "every member's own step graph launched at once on its own stream"},
             "streams": {"value": vc, "unit": "cell-updates/s", "ms_per_step": ms_c / args.steps,
                         "steps": args.steps,
                         "mode": "every member launched at once from the host on its own streams"},
             "plain": {"value": vp, "unit": "cell-updates/s", "ms_per_step": ms_p / n_p, "steps": n_p,
                       "mode": "members one after another, kernels launched from the host loop"},
-            "graph_over_plain": vg / vp, "streams_over_plain": vc / vp}
+            "graph_over_plain": vg / vp, "member_graphs_over_plain": vm / vp, "streams_over_plain": vc / vp}
 
 
 KERNELS = {  # id: (name, launches per box-step)

@@ -298,8 +298,9 @@ class Ensemble:
     def run(self, nsteps: int, graph: bool = True, concurrent: bool = False):
         """graph: one CUDA graph per main step for all members; concurrent
         (without graph): every member launched at once on its own stream;
-        neither: members one after another."""
-        mode = 1 if graph else (2 if concurrent else 0)
+        both: every member's own step graph launched at once on its own
+        stream; neither: members one after another."""
+        mode = (3 if concurrent else 1) if graph else (2 if concurrent else 0)
         self.ctx.check(self.L.g3m3_ensemble_run(self.h, nsteps, mode))
 
     def stats(self):

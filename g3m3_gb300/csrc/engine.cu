@@ -78,6 +78,10 @@ struct g3m3_model {
   cudaStream_t divb_stream[G3M3_MAX_GRIDS] = {};
   cudaEvent_t divb_ev[G3M3_MAX_GRIDS] = {};
   int cg_hint_box[G3M3_MAX_GRIDS] = {};
+  CgRun divb_run[G3M3_MAX_GRIDS];      // the pass in flight (divb_begin / divb_poll / divb_end)
+  int divb_rep[G3M3_MAX_GRIDS] = {};
+  bool divb_fin[G3M3_MAX_GRIDS] = {};
+  int divb_worst = 0;
   // host-fed step (g3m3_model_step_host): the state to upload while the
   // next step is enqueued, box by box on a copy stream
   const float* up_src = nullptr;
@@ -741,12 +745,19 @@ int step_enqueue(g3m3_model* m, const std::vector<Action>& acts) {
 }
 
 // After the step's work completed: next time steps, div B when due.
-int step_finish(g3m3_model* m) {
+// With `due`, the pass is left to the caller and *due says whether one is
+// due now.
+int step_finish(g3m3_model* m, bool* due = nullptr) {
   cudaError_t e;
   if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(m->ctx, e, "main step");
   finish_steps(m, 1, m->p.n_grids);
   m->nsteps_done += 1;
-  if (m->p.divb_every > 0 && (m->nsteps_done % m->p.divb_every) == 0) {
+  const bool now = m->p.divb_every > 0 && (m->nsteps_done % m->p.divb_every) == 0;
+  if (due) {
+    *due = now;
+    return G3M3_OK;
+  }
+  if (now) {
     const int st = g3m3_model_divb_all(m);
     if (st && st != G3M3_ERR_NOCONV) return st;
     if ((e = cudaStreamSynchronize(S(m))) != cudaSuccess) return cuda_check(m->ctx, e, "divb");
@@ -1009,25 +1020,23 @@ int ensure_divb_boxes(g3m3_model* m) {
   return G3M3_OK;
 }
 
-}  // namespace
-
 // divB_correct twice per box (3d_main.f90:1067-1096, 3363-3408), then the
 // fine boxes' B copied onto the coarse ones.  A box's solves touch only its
 // own B, so the boxes run side by side, each on its own stream with its own
 // solver state and vectors; every solve is the same sequence of kernels as
-// one run alone.
-int g3m3_model_divb_all(g3m3_model* m) {
-  if (!m) return G3M3_ERR_ARG;
+// one run alone.  The pass is split into divb_begin (queue every box's
+// first solve), divb_poll (advance every unfinished solve once; a box's
+// second solve starts when its first has ended) and divb_end (join the box
+// streams, flanks_synced and corer), so that an ensemble can keep the
+// passes of all its members in flight together.
+int divb_begin(g3m3_model* m) {
   const g3m3_params& p = m->p;
   const int ng = p.n_grids;
   int st = ensure_divb_boxes(m);
   if (st) return st;
   G3M3_CUDA(m->ctx, cudaEventRecord(m->fork_ev, S(m)));
-  CgRun run[G3M3_MAX_GRIDS];
-  int rep[G3M3_MAX_GRIDS] = {};
-  bool fin[G3M3_MAX_GRIDS] = {};
   for (int b = 1; b <= ng; b++) {
-    CgRun& r = run[b - 1];
+    CgRun& r = m->divb_run[b - 1];
     DivbArgs& a = r.a;
     a = DivbArgs{};
     a.bx = C(m, G3M3_F_BX, b); a.by = C(m, G3M3_F_BY, b); a.bz = C(m, G3M3_F_BZ, b);
@@ -1039,39 +1048,53 @@ int g3m3_model_divb_all(g3m3_model* m) {
     a.rx = a.ry = a.rz = p.xspac[b - 1];
     r.host_st = m->host_cg_box + (b - 1);
     r.s = m->divb_stream[b - 1];
+    m->divb_rep[b - 1] = 0;
+    m->divb_fin[b - 1] = false;
     G3M3_CUDA(m->ctx, cudaStreamWaitEvent(r.s, m->fork_ev, 0));
   }
+  m->divb_worst = G3M3_OK;
   for (int b = ng; b >= 1; b--) {
     const int h = m->cg_hint_box[b - 1] > 0 ? m->cg_hint_box[b - 1] : m->ctx->cg_hint;
-    if ((st = cg_begin(m->ctx, run[b - 1], p.divb_errlim, false, 1, h))) return st;
+    if ((st = cg_begin(m->ctx, m->divb_run[b - 1], p.divb_errlim, false, 1, h))) return st;
   }
-  int worst = G3M3_OK;
-  for (bool busy = true; busy;) {
-    busy = false;
-    for (int b = ng; b >= 1; b--) {
-      if (fin[b - 1]) continue;
-      busy = true;
-      CgRun& r = run[b - 1];
-      bool done = false;
-      if ((st = cg_step(m->ctx, r, &done))) return st;
-      if (!done) continue;
-      const int iters = r.host_st->iters;
-      if (r.status == CG_CONVERGED && iters > 0 && iters <= 4096) m->cg_hint_box[b - 1] = iters;
-      if (r.status == CG_MAXIT) worst = G3M3_ERR_NOCONV;
-      divb_launch_apply(r.a, r.s);
-      if (rep[b - 1] == 0) {
-        rep[b - 1] = 1;
-        const int h = m->cg_hint_box[b - 1] > 0 ? m->cg_hint_box[b - 1] : m->ctx->cg_hint;
-        if ((st = cg_begin(m->ctx, r, p.divb_errlim, false, 1, h))) return st;
-      } else {
-        fin[b - 1] = true;
-      }
+  return G3M3_OK;
+}
+
+int divb_poll(g3m3_model* m, bool* all_done) {
+  const g3m3_params& p = m->p;
+  const int ng = p.n_grids;
+  int st;
+  *all_done = true;
+  for (int b = ng; b >= 1; b--) {
+    if (m->divb_fin[b - 1]) continue;
+    *all_done = false;
+    CgRun& r = m->divb_run[b - 1];
+    bool done = false;
+    if ((st = cg_step(m->ctx, r, &done))) return st;
+    if (!done) continue;
+    const int iters = r.host_st->iters;
+    if (r.status == CG_CONVERGED && iters > 0 && iters <= 4096) m->cg_hint_box[b - 1] = iters;
+    if (r.status == CG_MAXIT) m->divb_worst = G3M3_ERR_NOCONV;
+    divb_launch_apply(r.a, r.s);
+    if (m->divb_rep[b - 1] == 0) {
+      m->divb_rep[b - 1] = 1;
+      const int h = m->cg_hint_box[b - 1] > 0 ? m->cg_hint_box[b - 1] : m->ctx->cg_hint;
+      if ((st = cg_begin(m->ctx, r, p.divb_errlim, false, 1, h))) return st;
+    } else {
+      m->divb_fin[b - 1] = true;
     }
   }
+  return G3M3_OK;
+}
+
+int divb_end(g3m3_model* m) {
+  const g3m3_params& p = m->p;
+  const int ng = p.n_grids;
   for (int b = 1; b <= ng; b++) {
-    G3M3_CUDA(m->ctx, cudaEventRecord(m->divb_ev[b - 1], run[b - 1].s));
+    G3M3_CUDA(m->ctx, cudaEventRecord(m->divb_ev[b - 1], m->divb_run[b - 1].s));
     G3M3_CUDA(m->ctx, cudaStreamWaitEvent(S(m), m->divb_ev[b - 1], 0));
   }
+  const int worst = m->divb_worst;
   if (worst) set_err(m->ctx, worst, "div B solver: too many iterations");
   for (int b = ng - 1; b >= 1; b--) {
     SyncedArgs a{};
@@ -1090,9 +1113,50 @@ int g3m3_model_divb_all(g3m3_model* m) {
   return worst;
 }
 
+}  // namespace
+
+int g3m3_model_divb_all(g3m3_model* m) {
+  if (!m) return G3M3_ERR_ARG;
+  int st = divb_begin(m);
+  for (bool done = false; !st && !done;) st = divb_poll(m, &done);
+  return st ? st : divb_end(m);
+}
+
 namespace {
 
 // One main step: plan, enqueue or replay, wait, finish (div B when due).
+// The step graph of a planned main step: from the model's cache (keyed by
+// buffer roles + actions), or captured on the model's stream -- scalar
+// upload from the pinned table, the step, and the read-back of the recorded
+// maxima -- and instantiated.
+int step_graph(g3m3_model* m, const std::vector<Action>& acts, const std::string& key, cudaGraphExec_t* out) {
+  auto found = m->graphs.find(key);
+  if (found == m->graphs.end()) {
+    cudaStream_t s = S(m);
+    cudaError_t e;
+    Roles saved = save_roles(m);
+    cudaGraph_t g = nullptr;
+    if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+      return cuda_check(m->ctx, e, "begin capture");
+    const int rc = step_enqueue(m, acts);
+    cudaError_t e2 = cudaStreamEndCapture(s, &g);
+    restore_roles(m, saved);   // capture did not run anything
+    if (rc || e2 != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      if (rc) return rc;
+      return cuda_check(m->ctx, e2, "graph capture");
+    }
+    cudaGraphExec_t ex = nullptr;
+    e = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_check(m->ctx, e, "graph instantiate");
+    found = m->graphs.emplace(key, ex).first;
+    m->kernel_nodes[key] = m->launches_in_step;
+  }
+  *out = found->second;
+  return G3M3_OK;
+}
+
 int one_step(g3m3_model* m, int use_graph, std::vector<Action>& acts) {
   cudaStream_t s = S(m);
   std::string key;
@@ -1105,30 +1169,9 @@ int one_step(g3m3_model* m, int use_graph, std::vector<Action>& acts) {
   }
   cudaError_t e;
   if (use_graph) {
-    auto found = m->graphs.find(key);
-    if (found == m->graphs.end()) {
-      // capture: scalar upload from the pinned table, the step, and the
-      // read-back of the recorded maxima
-      Roles saved = save_roles(m);
-      cudaGraph_t g = nullptr;
-      if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
-        return cuda_check(m->ctx, e, "begin capture");
-      rc = step_enqueue(m, acts);
-      cudaError_t e2 = cudaStreamEndCapture(s, &g);
-      restore_roles(m, saved);   // capture did not run anything
-      if (rc || e2 != cudaSuccess) {
-        if (g) cudaGraphDestroy(g);
-        if (rc) return rc;
-        return cuda_check(m->ctx, e2, "graph capture");
-      }
-      cudaGraphExec_t ex = nullptr;
-      e = cudaGraphInstantiate(&ex, g, 0);
-      cudaGraphDestroy(g);
-      if (e != cudaSuccess) return cuda_check(m->ctx, e, "graph instantiate");
-      found = m->graphs.emplace(key, ex).first;
-      m->kernel_nodes[key] = m->launches_in_step;
-    }
-    if ((e = cudaGraphLaunch(found->second, s)) != cudaSuccess) return cuda_check(m->ctx, e, "graph launch");
+    cudaGraphExec_t ex = nullptr;
+    if ((rc = step_graph(m, acts, key, &ex))) return rc;
+    if ((e = cudaGraphLaunch(ex, s)) != cudaSuccess) return cuda_check(m->ctx, e, "graph launch");
     apply_role_swaps(m, acts);
     m->graph_launches += 1;
     m->kernels += m->kernel_nodes[key];
@@ -1753,26 +1796,92 @@ int g3m3_ensemble_member(g3m3_ensemble* e, int i, g3m3_model** out) {
 
 void* g3m3_ensemble_stream(g3m3_ensemble* e) { return e ? (void*)e->ctx->stream : nullptr; }
 
+namespace {
+
+// The members' step ends; the div B passes that are due run together, every
+// member's boxes solving side by side (their results are those of each
+// member alone).
+int finish_members(g3m3_ensemble* e) {
+  const size_t nm = e->members.size();
+  std::vector<char> due(nm, 0);
+  bool any = false;
+  for (size_t i = 0; i < nm; i++) {
+    bool d = false;
+    if (int rc = step_finish(e->members[i], &d)) return rc;
+    due[i] = d;
+    any = any || d;
+  }
+  if (!any) return G3M3_OK;
+  for (size_t i = 0; i < nm; i++)
+    if (due[i])
+      if (int rc = divb_begin(e->members[i])) return rc;
+  for (bool busy = true; busy;) {
+    busy = false;
+    for (size_t i = 0; i < nm; i++) {
+      if (!due[i]) continue;
+      bool done = false;
+      if (int rc = divb_poll(e->members[i], &done)) return rc;
+      if (done) due[i] = 2;   // polled to the end: joined below
+      else busy = true;
+    }
+    for (size_t i = 0; i < nm; i++)
+      if (due[i] == 2) {
+        g3m3_model* m = e->members[i];
+        const int rc = divb_end(m);
+        if (rc && rc != G3M3_ERR_NOCONV) return rc;
+        cudaError_t ce = cudaStreamSynchronize(S(m));
+        if (ce != cudaSuccess) return cuda_check(e->ctx, ce, "divb");
+        due[i] = 0;
+      }
+  }
+  return G3M3_OK;
+}
+
+}  // namespace
+
 int g3m3_ensemble_run(g3m3_ensemble* e, int nsteps, int use_graph) {
-  if (!e || nsteps < 0 || use_graph < 0 || use_graph > 2) return G3M3_ERR_ARG;
+  if (!e || nsteps < 0 || use_graph < 0 || use_graph > 3) return G3M3_ERR_ARG;
   // 0: members one after another; 1: one graph per main step; 2: every
-  // member launched from the host on its own stream, all at once
+  // member launched from the host on its own stream, all at once; 3: every
+  // member's own step graph launched on its own stream, all at once
+  const bool member_graphs = use_graph == 3;
   const bool concurrent = use_graph == 2;
-  if (use_graph == 2) use_graph = 0;
+  if (use_graph == 2 || use_graph == 3) use_graph = 0;
   const size_t nm = e->members.size();
   cudaStream_t origin = e->ctx->stream;
   e->kernels = 0;
   e->graph_launches = 0;
   std::vector<std::vector<Action>> acts(nm);
+  std::vector<std::string> keys(nm);
   cudaError_t ce;
   for (int it = 0; it < nsteps; it++) {
     std::string key;
     for (size_t i = 0; i < nm; i++) {
-      std::string k;
-      const int rc = step_plan(e->members[i], acts[i], k);
+      const int rc = step_plan(e->members[i], acts[i], keys[i]);
       if (rc) return rc;
-      key += k;
+      key += keys[i];
       key += '|';
+    }
+    if (member_graphs) {
+      // find or capture every member's graph first (captures are isolated),
+      // then launch them all between the fork and join events
+      std::vector<cudaGraphExec_t> ex(nm);
+      for (size_t i = 0; i < nm; i++)
+        if (int rc = step_graph(e->members[i], acts[i], keys[i], &ex[i])) return rc;
+      if ((ce = cudaEventRecord(e->fork, origin)) != cudaSuccess) return cuda_check(e->ctx, ce, "fork");
+      for (size_t i = 0; i < nm; i++) {
+        g3m3_model* m = e->members[i];
+        if ((ce = cudaStreamWaitEvent(S(m), e->fork, 0)) != cudaSuccess) return cuda_check(e->ctx, ce, "fork");
+        if ((ce = cudaGraphLaunch(ex[i], S(m))) != cudaSuccess) return cuda_check(e->ctx, ce, "graph launch");
+        apply_role_swaps(m, acts[i]);
+        e->kernels += m->kernel_nodes[keys[i]];
+        e->graph_launches += 1;
+        if ((ce = cudaEventRecord(e->done[i], S(m))) != cudaSuccess) return cuda_check(e->ctx, ce, "join");
+        if ((ce = cudaStreamWaitEvent(origin, e->done[i], 0)) != cudaSuccess) return cuda_check(e->ctx, ce, "join");
+      }
+      if ((ce = cudaStreamSynchronize(origin)) != cudaSuccess) return cuda_check(e->ctx, ce, "ensemble step");
+      if (int rc = finish_members(e)) return rc;
+      continue;
     }
     // every member's step is ordered after earlier work on the ensemble's
     // stream and the ensemble's stream after every member's step, so events
@@ -1828,10 +1937,7 @@ int g3m3_ensemble_run(g3m3_ensemble* e, int nsteps, int use_graph) {
       if (rc) return rc;
     }
     if ((ce = cudaStreamSynchronize(origin)) != cudaSuccess) return cuda_check(e->ctx, ce, "ensemble step");
-    for (size_t i = 0; i < nm; i++) {
-      const int rc = step_finish(e->members[i]);
-      if (rc) return rc;
-    }
+    if (int rc = finish_members(e)) return rc;
   }
   return G3M3_OK;
 }

@@ -501,7 +501,9 @@ int g3m3_model_time_kernel(g3m3_model* m, int kernel, int box, int reps,
  * use_graph = 1, one main step of all members is one CUDA graph (members on
  * their own streams, overlapping on the GPU); 0, the members step one after
  * another from the host loop; 2, every member's kernels are launched from
- * the host on the member's own stream, all members at once.  Results are those of running each
+ * the host on the member's own stream, all members at once; 3, every
+ * member's own step graph (the one g3m3_model_run captures) is launched on
+ * the member's own stream, all members at once.  Results are those of running each
  * member alone.  Work is ordered after earlier work on the ensemble's
  * stream (the context's) and before later work there. */
 int g3m3_ensemble_create(g3m3_ctx* ctx, int n, const g3m3_params* params,
