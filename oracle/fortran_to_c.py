@@ -331,9 +331,9 @@ def split_top(s, sep=","):
             continue
         if ch in "'\"":
             q = ch
-        elif ch == "(":
+        elif ch in "([":
             depth += 1
-        elif ch == ")":
+        elif ch in ")]":
             depth -= 1
         if ch == sep and depth == 0:
             parts.append("".join(cur).strip())
@@ -374,6 +374,16 @@ RANK = {"logical": 0, "int": 1, "float": 2, "double": 3}
 SIZE = {"int": 4, "float": 4, "double": 8, "logical": 4, "char": 1}
 
 
+DEFERRED = ("deferred", None)     # a ':' bound of an allocatable array
+
+
+def pexpr(e):
+    """The AST of a parameter or initialiser, parsing lazy ones on use."""
+    if e is not None and e[0] == "lazy":
+        return parse_expr(e[1])
+    return e
+
+
 class Sym:
     def __init__(self, name):
         self.name = name
@@ -395,6 +405,8 @@ class Unit:
         self.implicit_none = False
         self.body = []            # (lineno, stmt) after the declarations
         self.commons = {}         # block -> [names in order]
+        self.uses = []            # modules named in USE statements
+        self.kind = "subroutine"  # or "program", "module"
 
     def sym(self, name):
         if name not in self.syms:
@@ -469,12 +481,16 @@ def _entity_dims(u, s):
         for d in split_top(dims[1:-1]):
             if d == "*":
                 dl.append((("int", "1"), None))
+            elif d.strip() == ":":
+                dl.append(DEFERRED)
             elif ":" in d and not d.startswith("("):
                 lo, hi = d.split(":", 1)
                 dl.append((parse_expr(lo), None if hi.strip() == "*" else parse_expr(hi)))
             else:
                 dl.append((("int", "1"), parse_expr(d)))
-    return name, dl, (parse_expr(init[1:]) if init else None)
+    # initialisers are parsed when used: some (array constructors, strings)
+    # are never needed
+    return name, dl, (("lazy", init[1:].strip()) if init else None)
 
 
 def declaration(u, st, ln):
@@ -506,7 +522,13 @@ def declaration(u, st, ln):
     if m:
         for ent in split_top(m.group(1)):
             name, val = ent.split("=", 1)
-            u.sym(name.strip()).param = parse_expr(val)
+            u.sym(name.strip()).param = ("lazy", val.strip())
+        return True
+    m = re.match(r"^use\s+(\w+)", st)
+    if m:
+        u.uses.append(m.group(1))
+        return True
+    if st.startswith("namelist"):
         return True
     m = _DECL.match(st)
     if not m:
@@ -533,7 +555,7 @@ def declaration(u, st, ln):
             is_param = True
         elif a.startswith("dimension"):
             _, adims, _ = _entity_dims(u, "x" + a[len("dimension"):])
-        elif a.startswith("intent") or a in ("save", "target", "optional"):
+        elif a.startswith("intent") or a in ("save", "target", "optional", "allocatable"):
             pass
         else:
             raise TranslateError(f"{u.name}: unsupported attribute {a!r}")
@@ -571,6 +593,7 @@ class Gen:
         self.tmp = 0
         self.loop = 0
         self.retyped = {}     # unit -> {dummy: type its callee reads it as}
+        self.main = False     # translating the main program's loop
         for u in units:
             self.layout_commons(u)
 
@@ -610,7 +633,8 @@ class Gen:
         if k == "name":
             s = u.syms.get(e[1])
             if s is not None and s.param is not None:
-                return self.eval_const(u, s.param)
+                v = self.eval_const(u, pexpr(s.param))
+                return int(v) if u.type_of(e[1]) == "int" else v
             raise TranslateError(f"{u.name}: {e[1]} is not a constant")
         if k == "ref" and e[1] == "kind":
             a = e[2][0]
@@ -706,22 +730,32 @@ class Gen:
     def name_ref(self, n):
         u = self.u
         s = u.syms.get(n)
-        if s is not None and s.param is not None:
-            v = self.eval_const(u, s.param)
+        if s is not None and s.param is not None and s.dims is None:
             t = u.type_of(n)
             if t == "int":
-                return str(int(v)), "int"
-            return (repr(float(v)) + ("f" if t == "float" else "")), t
+                return str(int(self.eval_const(u, pexpr(s.param)))), "int"
+            # a REAL parameter is its defining expression, converted once
+            c, _ = self.ex(pexpr(s.param))
+            return f"(({CTYPE[t]})({c}))", t
         t = u.type_of(n)
         if s is not None and s.dims is not None:
-            return f"{n}", t + "[]"
+            return self.cn(n), t + "[]"
         if s is not None and s.common is not None:
             blk, off = s.common
             return f"(*({CTYPE[t]}*)(ref_common_{blk} + {off}))", t
         if s is not None and s.is_dummy:
             return f"(*{n})", t
-        self.locals_used.add(n)
-        return n, t
+        if not n.startswith("s_"):
+            self.locals_used.add(n)
+        return self.cn(n), t
+
+    def cn(self, n):
+        """C name of a variable: the main program's variables are globals."""
+        if self.main and not n.startswith("s_"):
+            s = self.u.syms.get(n)
+            if s is None or (s.common is None and not s.is_dummy):
+                return "ref_main_" + n
+        return n
 
     def index(self, n, args):
         s = self.u.syms[n]
@@ -732,10 +766,10 @@ class Gen:
             c, t = self.ex(args[d])
             if t != "int":
                 raise TranslateError(f"{self.u.name}: non-integer subscript of {n}")
-            lo = f"{n}_lo{d}"
+            lo = f"{self.cn(n)}_lo{d}"
             term = f"((long)({c}) - {lo})"
             if terms:
-                terms = [f"({term} + {n}_ex{d} * {terms[0]})"]
+                terms = [f"({term} + {self.cn(n)}_ex{d} * {terms[0]})"]
             else:
                 terms = [term]
         return terms[0]
@@ -746,7 +780,7 @@ class Gen:
             if any(a[0] == "slice" for a in args):
                 raise TranslateError(f"{u.name}: array section {n} outside an assignment")
             t = u.type_of(n)
-            return f"{n}[{self.index(n, args)}]", t
+            return f"{self.cn(n)}[{self.index(n, args)}]", t
         return self.intrinsic(n, args)
 
     def intrinsic(self, n, args):
@@ -879,7 +913,8 @@ class Gen:
         opened = 0
         for i in range(rank - 1, -1, -1):
             d = loopvars[i][0]
-            out.append(f"{'  ' * body_ind}for (int s_{i} = (int){name}_lo{d}; s_{i} < (int)({name}_lo{d} + {name}_ex{d}); s_{i}++) {{")
+            cb = self.cn(name)
+            out.append(f"{'  ' * body_ind}for (int s_{i} = (int){cb}_lo{d}; s_{i} < (int)({cb}_lo{d} + {cb}_ex{d}); s_{i}++) {{")
             body_ind += 1
             opened += 1
         lc, lt = self.ex(lhs)
@@ -890,25 +925,63 @@ class Gen:
             out.append(f"{'  ' * body_ind}}}")
         del pad
 
+    def section_temp(self, e, ct, pre, post):
+        """An array section as an actual argument: a contiguous copy made
+        before the call and copied back after it (what a compiler does for a
+        non-contiguous section such as grid_minvals(1,:))."""
+        name, subs = e[1], e[2]
+        tmp = self.new_tmp()
+        cb = self.cn(name)
+        vars_, na = [], []
+        for d, sub in enumerate(subs):
+            if sub[0] == "slice":
+                if sub[1] is not None or sub[2] is not None:
+                    raise TranslateError(f"{self.u.name}: partial section of {name} as an argument")
+                v = f"s_{tmp}_{d}"
+                self.u.sym(v).type = "int"
+                vars_.append((d, v))
+                na.append(("name", v))
+            else:
+                na.append(sub)
+        elem, _ = self.ref(name, na)
+        size = " * ".join(f"{cb}_ex{d}" for d, _ in vars_)
+        pre.append(f"{ct}* {tmp} = ({ct}*)malloc(sizeof({ct}) * (size_t)({size})); long n_{tmp} = 0;")
+        loops_open, loops_close = "", ""
+        for d, v in reversed(vars_):
+            loops_open += f"for (int {v} = (int){cb}_lo{d}; {v} < (int)({cb}_lo{d} + {cb}_ex{d}); {v}++) "
+        pre.append(loops_open + f"{tmp}[n_{tmp}++] = {elem};")
+        post.append(f"n_{tmp} = 0; " + loops_open + f"{elem} = {tmp}[n_{tmp}++];")
+        post.append(f"free({tmp});")
+        return tmp
+
     def call(self, name, argstr, out, ind):
         pad = "  " * ind
         if name not in self.units:
-            raise TranslateError(f"{self.u.name}: call to {name}, which is not translated")
+            if not self.main:
+                raise TranslateError(f"{self.u.name}: call to {name}, which is not translated")
+            # the main loop's calls outside the hot path are recorded, not run
+            out.append(f'{pad}ref_untranslated("{name}");')
+            return
         callee = self.units[name]
         actuals = split_top(argstr) if argstr.strip() else []
         if len(actuals) != len(callee.args):
             raise TranslateError(f"{self.u.name}: call {name} with {len(actuals)} of {len(callee.args)} arguments")
-        pre, cargs = [], []
+        pre, cargs, post = [], [], []
         for a_s, dummy in zip(actuals, callee.args):
-            dt = callee.type_of(dummy)
+            # a dummy the callee only hands on is read as its callee's type
+            dt = self.retyped.get(name, {}).get(dummy, callee.type_of(dummy))
             e = parse_expr(a_s)
-            if e[0] == "name" and not (self.u.syms.get(e[1]) and self.u.syms[e[1]].param is not None):
+            if e[0] == "ref" and self.is_array(e[1]) and any(a[0] == "slice" for a in e[2]):
+                cargs.append(self.section_temp(e, CTYPE[self.u.type_of(e[1])], pre, post))
+                continue
+            sym = self.u.syms.get(e[1]) if e[0] == "name" else None
+            if e[0] == "name" and not (sym is not None and sym.param is not None and sym.dims is None):
                 c, t = self.name_ref(e[1])
                 if t.endswith("[]"):
-                    cargs.append(e[1])
+                    cargs.append(c)
                     continue
                 s = self.u.syms.get(e[1])
-                if t != dt:
+                if CTYPE[t] != CTYPE[dt]:
                     # Without interfaces the compiler passes the address and
                     # the callee reads it as its own type.  A dummy handed on
                     # unread keeps the caller's bits (bndry_flanks declares
@@ -920,9 +993,13 @@ class Gen:
                     self.retyped.setdefault(self.u.name, {})[e[1]] = dt
                     continue
                 if s is not None and s.is_dummy and s.common is None:
-                    cargs.append(e[1])
+                    arg = e[1]
                 else:
-                    cargs.append(f"&{c}" if not c.startswith("(*") else c[2:-1])
+                    arg = f"&{c}" if not c.startswith("(*") else c[2:-1]
+                declared = CTYPE[callee.type_of(dummy)]
+                if declared != CTYPE[dt]:      # the callee only hands it on
+                    arg = f"({declared}*){arg}"
+                cargs.append(arg)
                 continue
             if e[0] == "ref" and self.is_array(e[1]):
                 c, t = self.ref(e[1], e[2])
@@ -932,7 +1009,8 @@ class Gen:
             tmp = self.new_tmp()
             pre.append(f"{CTYPE[dt]} {tmp} = ({CTYPE[dt]})({c});")
             cargs.append(f"&{tmp}")
-        out.append(pad + "{ " + " ".join(pre) + f" ref_{name}(" + ", ".join(cargs) + "); }")
+        out.append(pad + "{ " + " ".join(pre) + f" ref_{name}(" + ", ".join(cargs) + "); "
+                   + " ".join(post) + " }")
 
     def body(self, u):
         out = []
@@ -1036,10 +1114,10 @@ class Gen:
         if st == "continue":
             out.append(f"{pad};")
             return
-        if st.startswith("stop"):
+        if st.startswith("stop") or st.startswith("call exit"):
             out.append(f'{pad}ref_stop("{u.name}");')
             return
-        if re.match(r"^(write|print)\b", st):
+        if re.match(r"^(write|print|open|close|read|inquire|rewind|backspace|flush)\b", st):
             out.append(f"{pad}/* output statement dropped */")
             return
         m = re.match(r"^call\s+(\w+)\s*(\((.*)\))?\s*$", st)
@@ -1099,7 +1177,7 @@ class Gen:
             t = u.type_of(name)
             ct = CTYPE[t]
             if s.dims is None:
-                init = self.ex(s.init)[0] if s.init is not None else "0"
+                init = self.ex(pexpr(s.init))[0] if s.init is not None else "0"
                 decl.append(f"  static {ct} {name} = {init};")
                 saved_reset.append(f"{name}_reset")
                 continue
@@ -1162,7 +1240,22 @@ class Gen:
             "static inline double ref_powid(double x, int n) { double r = 1.0; int k = n < 0 ? -n : n;"
             " for (int i = 0; i < k; i++) r = r * x; return n < 0 ? 1.0 / r : r; }",
             "static inline int ref_powii(int x, int n) { int r = 1; for (int i = 0; i < n; i++) r *= x; return r; }",
-            "static void ref_stop(const char* who) { fprintf(stderr, \"STOP in %s\\n\", who); exit(3); }",
+            "#include <setjmp.h>",
+            "int ref_main_stopped = 0;",
+            "int ref_untranslated_calls = 0;",
+            "char ref_untranslated_last[64];",
+            "static jmp_buf ref_jmp;",
+            "static int ref_jmp_armed = 0;",
+            "static void ref_stop(const char* who) {",
+            "  fprintf(stderr, \"STOP in %s\\n\", who);",
+            "  ref_main_stopped = 1;",
+            "  if (ref_jmp_armed) longjmp(ref_jmp, 1);",
+            "  exit(3);",
+            "}",
+            "static void ref_untranslated(const char* who) {",
+            "  ref_untranslated_calls++;",
+            "  strncpy(ref_untranslated_last, who, sizeof ref_untranslated_last - 1);",
+            "}",
         ]
         for blk, (size, _) in sorted(self.commons.items()):
             out.append(f"unsigned char ref_common_{blk}[{max(size, 8)}] __attribute__((aligned(16)));")
@@ -1177,6 +1270,102 @@ class Gen:
             out += code
         del resets
         return out
+
+    def main_unit(self, u):
+        """One C function running the time loop's body *nsteps times, the
+        main program's variables as exported globals ref_main_<name>."""
+        self.u = u
+        self.main = True
+        self.locals_used = set()
+        body = self.body(u)
+        loop_body = u.body
+        u.body = u.init_body
+        init_body = self.body(u)
+        u.body = loop_body
+        for n in self.locals_used:
+            u.sym(n)
+        glob, prolog, meta = [], [], {}
+        for name, sym in sorted(u.syms.items()):
+            if (sym.param is not None and sym.dims is None) or name.startswith("s_"):
+                continue
+            self.where = (u.src, "declaration of", name)
+            t = u.type_of(name)
+            ct = CTYPE[t]
+            if t == "char":        # names and formats of files: not on the path
+                continue
+            if sym.param is not None:
+                # a PARAMETER array from an array constructor [a, b, ...]
+                src = sym.param[1].strip()
+                if src.startswith("(/"):
+                    src = "[" + src[2:-2] + "]"
+                if not (src.startswith("[") and src.endswith("]")):
+                    raise TranslateError(f"parameter array {name}: {src!r}")
+                vals = [self.ex(parse_expr(v))[0] for v in split_top(src[1:-1])]
+                g = "ref_main_" + name
+                glob.append(f"{ct} {g}[{len(vals)}] = {{{', '.join(vals)}}};")
+                glob.append(f"const long {g}_lo0 = 1;")
+                glob.append(f"const long {g}_ex0 = {len(vals)};")
+                continue
+            if sym.common is not None:
+                if sym.dims is not None:
+                    blk, off = sym.common
+                    prolog.append(f"  {ct}* {name} = ({ct}*)(ref_common_{blk} + {off});")
+                    for d, (lo, hi) in enumerate(sym.dims):
+                        prolog.append(f"  const long {name}_lo{d} = {self.ex(lo)[0]};")
+                        prolog.append(f"  const long {name}_ex{d} = (long)({self.ex(hi)[0]}) - {name}_lo{d} + 1;")
+                continue
+            g = "ref_main_" + name
+            if sym.dims is None:
+                init = self.ex(pexpr(sym.init))[0] if sym.init is not None else "0"
+                glob.append(f"{ct} {g} = {init};")
+                meta[name] = {"type": t, "dims": None}
+            elif any(d is DEFERRED or d == DEFERRED for d in sym.dims):
+                glob.append(f"{ct}* {g} = 0;")
+                for d in range(len(sym.dims)):
+                    glob.append(f"long {g}_lo{d} = 1;")
+                    glob.append(f"long {g}_ex{d} = 0;")
+                meta[name] = {"type": t, "dims": "allocatable", "rank": len(sym.dims)}
+            else:
+                ext = []
+                for d, (lo, hi) in enumerate(sym.dims):
+                    l0 = self.const_int(u, lo)
+                    e = self.const_int(u, hi) - l0 + 1
+                    ext.append(e)
+                    glob.append(f"const long {g}_lo{d} = {l0};")
+                    glob.append(f"const long {g}_ex{d} = {e};")
+                n = 1
+                for e in ext:
+                    n *= e
+                # a guard of zeros on both sides: the loop reads t_old(0)
+                # and t_new(0) (box - 1 with box = 1)
+                glob.append(f"{ct} {g}_mem[{n + 16}] __attribute__((aligned(16)));")
+                glob.append(f"{ct}* const {g} = {g}_mem + 8;")
+                meta[name] = {"type": t, "dims": ext}
+        out = [f"/* ---- {u.src}: the body of the time loop, lines {u.loop_lines[0]}-{u.loop_lines[1]} ---- */"]
+        out += glob
+        out.append(f"/* the time-step set-up before the loop, lines {u.init_lines[0]}-{u.init_lines[1]} */")
+        out.append("void ref_main_init_steps(void) {")
+        out += prolog
+        out.append("  if (setjmp(ref_jmp)) { ref_jmp_armed = 0; return; }")
+        out.append("  ref_jmp_armed = 1;")
+        out += init_body
+        out.append("  goto L_return;")
+        out.append("L_return:;")
+        out.append("  ref_jmp_armed = 0;")
+        out.append("}")
+        out.append("void ref_main_steps(int* nsteps) {")
+        out += prolog
+        out.append("  if (setjmp(ref_jmp)) { ref_jmp_armed = 0; return; }")
+        out.append("  ref_jmp_armed = 1;")
+        out.append("  for (int it_ = 0; it_ < *nsteps; it_++) {")
+        out += body
+        out.append("  }")
+        out.append("  goto L_return;")
+        out.append("L_return:;")
+        out.append("  ref_jmp_armed = 0;")
+        out.append("}")
+        self.main = False
+        return out, meta
 
     def meta(self, order):
         subs = {}
@@ -1193,6 +1382,89 @@ class Gen:
             {"name": n, "type": t, "offset": off, "count": c} for n, t, off, c in mem]}
             for blk, (size, mem) in self.commons.items()}
         return {"subroutines": subs, "commons": commons}
+
+
+_DO_START = re.compile(r"^do(\s+while\b|\s+\w+\s*=)")
+_DO_END = re.compile(r"^end\s*do$")
+
+
+def parse_module_params(path, into):
+    """The declarations of a module up to CONTAINS, merged into unit `into`
+    where it declares nothing of the same name (USE association)."""
+    text = open(path, encoding="latin-1").read()
+    m = Unit("module", [], os.path.basename(path))
+    for ln, st in statements(text):
+        if st.startswith("module ") or st == "implicit none":
+            continue
+        if st == "contains" or st.startswith("end module"):
+            break
+        if not declaration(m, st, ln):
+            raise TranslateError(f"{path}:{ln}: unexpected statement in module: {st!r}")
+    for n, sym in m.syms.items():
+        if n not in into.syms or into.syms[n].type is None:
+            into.syms[n] = sym
+
+
+def parse_main_loop(path, module_dir, overrides):
+    """The main program's declarations and the body of its time loop
+    ``do while(t.lt.tmax)`` (code/3d_main.f90), as a unit whose variables
+    become C globals.  `overrides` replaces PARAMETER values (grid size)."""
+    text = open(path, encoding="latin-1").read()
+    sts = list(statements(text))
+    ln0, st0 = sts[0]
+    m = re.match(r"^program\s+(\w+)$", st0)
+    if not m:
+        raise TranslateError(f"{path}: does not start with PROGRAM")
+    u = Unit("main_steps", [], os.path.basename(path))
+    u.kind = "program"
+    i = 1
+    while i < len(sts) and declaration(u, sts[i][1], sts[i][0]):
+        i += 1
+    body = sts[i:]
+    start = next(j for j, (_, st) in enumerate(body)
+                 if re.match(r"^do\s+while\s*\(\s*t\s*\.lt\.\s*tmax\s*\)$", st))
+    depth = 0
+    for k in range(start, len(body)):
+        st = body[k][1]
+        if _DO_START.match(st):
+            depth += 1
+        elif _DO_END.match(st):
+            depth -= 1
+            if depth == 0:
+                break
+    else:
+        raise TranslateError("the time loop has no ENDDO")
+    u.body = body[start + 1:k]
+    u.loop_lines = (body[start][0], body[k][0])
+    # the time-step set-up just before the loop: the last top-level
+    # "do box=n_grids,1,-1" that checks densities and speeds of every box
+    depth, init = 0, None
+    for j in range(start):
+        st = body[j][1]
+        if depth == 0 and re.match(r"^do\s+box\s*=\s*n_grids\s*,\s*1\s*,\s*-1$", st):
+            d2 = 0
+            for e in range(j, start):
+                if _DO_START.match(body[e][1]):
+                    d2 += 1
+                elif _DO_END.match(body[e][1]):
+                    d2 -= 1
+                    if d2 == 0:
+                        break
+            if any(x[1].startswith("call set_speed_agrd") for x in body[j:e]):
+                init = (j, e)
+        if _DO_START.match(st):
+            depth += 1
+        elif _DO_END.match(st):
+            depth -= 1
+    if init is None:
+        raise TranslateError("no time-step set-up loop before the time loop")
+    u.init_body = body[init[0]:init[1] + 1]
+    u.init_lines = (body[init[0]][0], body[init[1]][0])
+    for mod in u.uses:
+        parse_module_params(os.path.join(module_dir, f"mod_{mod}.f90"), u)
+    for n, v in overrides.items():
+        u.sym(n).param = ("lazy", str(v))
+    return u
 
 
 def translate(code_dir, out_dir=OUT):
@@ -1216,11 +1488,55 @@ def translate(code_dir, out_dir=OUT):
     return cpath
 
 
-def compile_ref(out_dir=OUT, cc="gcc"):
-    cpath = os.path.join(out_dir, "g3m3_ref.c")
-    so = os.path.join(out_dir, "libg3m3_ref.so")
-    subprocess.run([cc, "-O2", "-fPIC", "-shared", "-std=gnu11", "-ffp-contract=off",
-                    "-fno-fast-math", "-fwrapv", "-w", "-o", so, cpath, "-lm"], check=True)
+# Grid sizes of the main-loop builds: the main program's PARAMETERs
+# limit (nx = ny = 2*limit+1, nz = limit+1), n_grids and mbndry.
+MAIN_CONFIGS = {
+    "tiny": {"limit": "8.", "n_grids": "1", "mbndry": "1"},
+    "tiny3": {"limit": "8.", "n_grids": "3", "mbndry": "1"},
+}
+
+
+def translate_main(code_dir, tag, overrides, out_dir=OUT):
+    """All routines plus the main program's time loop for one grid size:
+    g3m3_ref_main_<tag>.c and its variable list g3m3_ref_main_<tag>.json."""
+    units = []
+    for f in FILES:
+        units += parse_units(os.path.join(code_dir, f + ".f90"))
+    prog = parse_main_loop(os.path.join(code_dir, "3d_main.f90"), code_dir, overrides)
+    g = Gen(units)
+    g.layout_commons(prog)
+    order = [u.name for u in units]
+    g.where = None
+    try:
+        src = g.module(order)
+        main_src, main_meta = g.main_unit(prog)
+    except (TranslateError, KeyError, ValueError, IndexError, StopIteration) as e:
+        raise TranslateError(f"at {g.where}: {type(e).__name__}: {e}") from e
+    os.makedirs(out_dir, exist_ok=True)
+    cpath = os.path.join(out_dir, f"g3m3_ref_main_{tag}.c")
+    with open(cpath, "w") as fh:
+        fh.write("\n".join(src + main_src) + "\n")
+    meta = g.meta(order)
+    meta["main"] = {"variables": main_meta, "overrides": overrides,
+                    "loop_lines": list(prog.loop_lines), "init_lines": list(prog.init_lines)}
+    with open(os.path.join(out_dir, f"g3m3_ref_main_{tag}.json"), "w") as fh:
+        json.dump(meta, fh, indent=1)
+    return cpath
+
+
+def compile_ref(out_dir=OUT, cc="gcc", stem="g3m3_ref"):
+    cpath = os.path.join(out_dir, stem + ".c")
+    so = os.path.join(out_dir, "lib" + stem + ".so")
+    # warnings are not shown, but the ones that reveal a mistranslated
+    # argument (a pointer where a value belongs, or the reverse) are errors
+    r = subprocess.run([cc, "-O2", "-fPIC", "-shared", "-std=gnu11", "-ffp-contract=off",
+                        "-fno-fast-math", "-fwrapv", "-Werror=int-conversion",
+                        "-Werror=incompatible-pointer-types", "-Werror=implicit-function-declaration",
+                        "-Werror=pointer-to-int-cast", "-Werror=int-to-pointer-cast",
+                        "-o", so, cpath, "-lm"], capture_output=True, text=True)
+    if r.returncode:
+        errs = [ln for ln in r.stderr.splitlines() if "error" in ln]
+        raise TranslateError(f"{cpath} does not compile:\n" + "\n".join(errs[:20]))
     return so
 
 
@@ -1231,13 +1547,16 @@ def reference_code_dir():
 
 def main(argv):
     code_dir = argv[1] if len(argv) > 1 else reference_code_dir()
-    if not os.path.isdir(code_dir):
-        cpath = os.path.join(OUT, "g3m3_ref.c")
-        if os.path.exists(cpath):      # sources translated elsewhere travelled here
-            compile_ref()
-        return 0
-    translate(code_dir)
-    compile_ref()
+    stems = ["g3m3_ref"] + [f"g3m3_ref_main_{t}" for t in MAIN_CONFIGS]
+    if os.path.isdir(code_dir):
+        translate(code_dir)
+        for tag, ov in MAIN_CONFIGS.items():
+            translate_main(code_dir, tag, ov)
+    from concurrent.futures import ThreadPoolExecutor
+    todo = [st for st in stems if os.path.exists(os.path.join(OUT, st + ".c"))]
+    # sources translated elsewhere may have travelled here without the reference
+    with ThreadPoolExecutor(len(todo) or 1) as ex:
+        list(ex.map(lambda st: compile_ref(stem=st), todo))
     return 0
 
 

@@ -8,11 +8,15 @@
  * step schedule of code/3d_main.f90).  Every function cites the reference
  * lines it follows.
  *
- * PARITY UNPINNED: the reference ships no tests, golden vectors or fixtures
- * (code/test.f90 is an empty stub) and is Fortran, which no compiler in the
- * build image can build.  The restatement is held in place by analytic
- * known-answer tests (tests/test_oracle_kat.py) and by committed regression
- * fixtures (tests/golden/), not by outputs of the reference itself.
+ * PINNED TO THE REFERENCE: the reference ships no tests, golden vectors or
+ * fixtures (code/test.f90 is an empty stub) and is Fortran, for which the
+ * build image has no compiler; oracle/fortran_to_c.py translates its own
+ * routines and main loop to C (oracle/_ref, built from the sources where
+ * they lie, never committed), and every routine here, the time-step set-up
+ * and the main step agree with that build bitwise (tests/test_ref_pin.py,
+ * tests/test_ref_main.py).  Analytic known-answer tests
+ * (tests/test_oracle_kat.py) and the reference-made digests of
+ * tests/golden/ hold it where the sources are absent.
  *
  * Conventions: arrays are column-major FP32 exactly as in the reference,
  * (nx,ny,nz,n_grids) with a 1-based box index, or (nx,ny,nz) for per-box

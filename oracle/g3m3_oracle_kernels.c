@@ -3,8 +3,8 @@
  * per-box routines of the G3M^3 step (reference rows a1-a19).  Only the test
  * suite, the smoke check and bench.py's CPU-baseline leg use it.
  *
- * PARITY UNPINNED (no reference outputs exist to pin it; see
- * g3m3_oracle.h).  Each function follows the cited Fortran statement for
+ * Pinned bitwise to the reference's own routines, translated from its
+ * Fortran and compiled (see g3m3_oracle.h).  Each function follows the cited Fortran statement for
  * statement; float literals keep every operation in FP32 and the operand
  * order of the source is kept.  Loops whose iterations are independent carry
  * an OpenMP pragma: with or without -fopenmp they give identical bits.

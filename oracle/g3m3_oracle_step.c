@@ -1,8 +1,8 @@
 /*
  * g3m3_oracle_step.c -- TEST INFRASTRUCTURE: CPU restatement of the
  * boundary routines, the div B cleaner and the main-step schedule of the
- * G3M^3 reference (rows a13, a14, a18, a20).  PARITY UNPINNED (see
- * g3m3_oracle.h).
+ * G3M^3 reference (rows a13, a14, a18, a20).  Pinned bitwise to the
+ * reference's own routines and main loop (see g3m3_oracle.h).
  */
 #include <math.h>
 #include <stddef.h>

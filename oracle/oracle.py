@@ -3,7 +3,7 @@
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg may
 import this module.  It loads liboracle.so (serial, the parity reference) or
 liboracle_omp.so (OpenMP, the timed baseline); both give identical bits.
-PARITY UNPINNED: see g3m3_oracle.h.
+Pinned to the reference's own routines and main loop: see g3m3_oracle.h.
 """
 from __future__ import annotations
 

@@ -1,0 +1,159 @@
+"""ctypes access to oracle/_ref/libg3m3_ref_main_<tag>.so: the reference's
+main time loop (the body of ``do while(t.lt.tmax)``, code/3d_main.f90),
+translated to C with all its routines by oracle/fortran_to_c.py for one grid
+size.  TEST INFRASTRUCTURE ONLY.
+
+The main program's variables are globals ``ref_main_<name>``; this module
+loads a state into them the way the reference's initialisation leaves it,
+runs main steps, and reads the fields back.  Everything outside the hot path
+stays off: no spacecraft, no fluid input, no tilting, no torus injection, no
+graphing; fluid-file times control the div B pass.
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+import os
+
+import numpy as np
+
+from _refpin import REF, load as load_routines
+from g3m3_gb300.params import FIELD_NAMES
+
+_CT = {"int": ctypes.c_int32, "logical": ctypes.c_int32, "float": ctypes.c_float,
+       "double": ctypes.c_double}
+_NP = {"int": np.int32, "logical": np.int32, "float": np.float32, "double": np.float64}
+BIG = 1.0e30
+
+
+class RefMain:
+    def __init__(self, tag):
+        so = os.path.join(REF, f"libg3m3_ref_main_{tag}.so")
+        if not os.path.exists(so):
+            load_routines()          # builds everything where the sources exist
+        if not os.path.exists(so):
+            raise FileNotFoundError(so)
+        self.lib = ctypes.CDLL(so)
+        with open(os.path.join(REF, f"g3m3_ref_main_{tag}.json")) as fh:
+            self.meta = json.load(fh)
+        self.vars = self.meta["main"]["variables"]
+        self.keep = []
+
+    # ---- variables ----
+    def _sym(self, name, ctype):
+        return ctype.in_dll(self.lib, "ref_main_" + name)
+
+    def set(self, **values):
+        for k, v in values.items():
+            if k not in self.vars:           # a member of one of the main program's commons
+                blk = next(b for b, d in self.meta["commons"].items()
+                           if any(m["name"] == k for m in d["members"]))
+                self.set_common(blk, **{k: v})
+                continue
+            m = self.vars[k]
+            if m["dims"] is not None:
+                raise TypeError(f"{k} is an array")
+            self._sym(k, _CT[m["type"]]).value = v
+
+    def get(self, name):
+        m = self.vars[name]
+        return self._sym(name, _CT[m["type"]]).value
+
+    def array(self, name):
+        """numpy view of a fixed-size array, C order (the Fortran dims reversed)."""
+        m = self.vars[name]
+        ptr = ctypes.c_void_p.in_dll(self.lib, "ref_main_" + name).value
+        n = int(np.prod(m["dims"]))
+        buf = (_CT[m["type"]] * n).from_address(ptr)
+        return np.ctypeslib.as_array(buf).reshape(tuple(reversed(m["dims"])))
+
+    def set_allocatable(self, name, arr, fdims):
+        """Point an ALLOCATABLE array at `arr` (C order of Fortran dims `fdims`)."""
+        m = self.vars[name]
+        a = np.ascontiguousarray(arr, dtype=_NP[m["type"]])
+        assert a.size == int(np.prod(fdims))
+        self.keep.append(a)
+        ctypes.c_void_p.in_dll(self.lib, "ref_main_" + name).value = a.ctypes.data
+        for d, e in enumerate(fdims):
+            ctypes.c_long.in_dll(self.lib, f"ref_main_{name}_lo{d}").value = 1
+            ctypes.c_long.in_dll(self.lib, f"ref_main_{name}_ex{d}").value = int(e)
+
+    def set_common(self, block, **values):
+        blk = self.meta["commons"][block]
+        base = ctypes.addressof(ctypes.c_ubyte.in_dll(self.lib, "ref_common_" + block))
+        members = {m["name"]: m for m in blk["members"]}
+        for k, v in values.items():
+            m = members[k]
+            a = np.ascontiguousarray(np.asarray(v, dtype=_NP[m["type"]]).ravel())
+            ctypes.memmove(base + m["offset"], a.ctypes.data, a.nbytes)
+
+    # ---- running ----
+    def init_steps(self):
+        """The reference's time-step set-up before its loop (density and
+        speed checks of every box, first t_stepnew)."""
+        self.lib.ref_main_init_steps()
+        self._check()
+
+    def steps(self, n):
+        self.lib.ref_main_steps.argtypes = [ctypes.c_void_p]
+        k = ctypes.c_int32(n)
+        self.lib.ref_main_steps(ctypes.addressof(k))
+        self._check()
+
+    def _check(self):
+        if ctypes.c_int.in_dll(self.lib, "ref_main_stopped").value:
+            raise RuntimeError("the reference's main loop executed STOP")
+        calls = ctypes.c_int.in_dll(self.lib, "ref_untranslated_calls").value
+        if calls:
+            last = ctypes.c_char.in_dll(self.lib, "ref_untranslated_last")
+            raise RuntimeError(f"{calls} calls to routines off the hot path "
+                               f"(last {ctypes.string_at(ctypes.addressof(last)).decode()})")
+
+    def load_state(self, p, cur, old, wrk, b0, resistive, lists, t, t_stepnew, divb_at=None):
+        """The state the reference's initialisation builds: fields, dipole,
+        resistivity, inner-boundary lists, grid, constants, times.  The div B
+        pass runs in the main step at which t first reaches `divb_at`."""
+        ng = p.n_grids
+        for q, name in enumerate(FIELD_NAMES):
+            self.array(name)[...] = cur[q]
+            self.array("old" + name)[...] = old[q]
+            self.array("wrk" + name)[...] = wrk[q]
+        for q, c in enumerate("xyz"):
+            self.array(f"b{c}0")[...] = b0[q]
+        res = self.array("resistive")
+        res[...] = resistive.reshape(res.shape)
+        for key in ("srf", "mid", "zero"):
+            ij = lists["ij" + key]            # C order (m, 3, mbndry) = Fortran (mbndry, 3, m)
+            self.set_allocatable("ij" + key, ij, (p.mbndry, 3, ij.shape[0]))
+            parm = lists["parm_" + key]
+            self.set_allocatable("parm_" + key, parm, (p.mbndry, 7, parm.shape[0]))
+            self.array("num" + key)[...] = lists["num" + key]
+            self.set(**{"m" + key: int(ij.shape[0])})
+        gmin, gmax = self.array("grid_minvals"), self.array("grid_maxvals")
+        for b in range(ng):
+            gmin[b] = [p.grd_xmin[b], p.grd_ymin[b], p.grd_zmin[b]]
+            gmax[b] = [p.grd_xmax[b], p.grd_ymax[b], p.grd_zmax[b]]
+        self.array("xspac")[...] = np.array(p.xspac[:ng], np.float32)
+        for k in ("rmassq", "rmassh", "rmasso", "gamma", "gamma1", "reynolds", "resist", "grav", "re_equiv",
+                  "chirho", "chipxyz", "chierg", "difrho", "diferg", "aniso_limit", "qvlim", "hvlim", "ovlim",
+                  "qclim", "hclim", "oclim", "cslim", "stepsz", "t_step_max", "srho", "rho_frac", "o_conc",
+                  "spress", "spx", "spy", "spz", "sbx_wind", "sby_wind", "sbz_wind", "ti_te", "erho", "epress",
+                  "alpha_e", "r_inner"):
+            self.set(**{k: float(getattr(p, k))})
+        self.set(isotropic=int(p.isotropic))
+        self.set_common("rotation", v_rot=p.v_rot, r_rot=p.r_rot)
+        # off the hot path
+        self.set(input_fluid=0, spacecraft=0, tilting=0, ringo=0, warp=0)
+        self.set(tmax=BIG, tgraph=BIG, tinj=BIG, dtilt=0.0, tilt=0.0)
+        self.set(t_equiv=1.0, planet_per=1.0, moon_per=1.0, moon_orbit_rad=0.0, moon_init_rot=0.0)
+        self.set(rho_equiv=1.0, v_equiv=1.0, planet_rad=1.0)
+        # fluid-file time: the div B pass runs there (3d_main.f90:3305-3408)
+        if divb_at is None:
+            self.set(ts1=BIG, divb_lores=0)
+        else:
+            self.set(ts1=float(divb_at), tsave=BIG, divb_lores=1, fluid_f=11, offset_f=0)
+        self.set(t=float(t))
+        self.array("t_stepnew")[...] = np.asarray(t_stepnew, np.float64)
+
+    def fields(self):
+        return np.stack([self.array(n) for n in FIELD_NAMES])

@@ -2,9 +2,10 @@
 state after 1 and 3 main steps of seeded small grids (one box 17x17x9; three
 nested boxes 17x17x9), with the time bookkeeping.
 
-The reference ships no golden data and cannot be compiled here (Fortran),
-so these digests pin the oracle restatement and the library to each other
-and to this committed record rather than to the reference itself.
+The reference ships no golden data; these digests are made by the oracle,
+and tests/test_ref_main.py checks that the reference's own set-up and main
+loop (translated and compiled by oracle/fortran_to_c.py) give exactly them,
+so the library's GPU test against them is a test against the reference.
 
     python tests/golden/make_golden.py
 """

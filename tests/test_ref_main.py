@@ -1,0 +1,112 @@
+"""The oracle's main step pinned to the reference's own main loop.
+
+The reference's time-step set-up and the body of its time loop
+(code/3d_main.f90, ``do while(t.lt.tmax)``), translated to C with every
+routine they call by oracle/fortran_to_c.py, run from a seeded state; the
+oracle's set-up and main step must give the same fields,
+time and next time steps bitwise -- on one box and on three nested,
+sub-cycled boxes, with and without the div B pass that the reference runs
+at a fluid-file time (FP32 dot products on both sides).  Runs on the CPU;
+skips where the reference's sources are absent.
+"""
+import numpy as np
+import pytest
+
+import _refpin
+from _support import assert_same, same_bits
+
+pytestmark = pytest.mark.skipif(_refpin.load() is None,
+                                reason="reference sources absent: oracle/_ref not built")
+
+
+def _pair(cfg, divb_at):
+    """The seeded state in both, after each side's time-step set-up (which
+    must agree too)."""
+    from _refmain import RefMain
+    from g3m3_gb300.state import make_config
+    from oracle.oracle import OracleModel
+    om = OracleModel(make_config(cfg))
+    rm = RefMain(cfg)
+    rm.load_state(om.p, om.cur, om.old, om.wrk, om.b0, om.resistive, om.lists, om.s.t,
+                  np.zeros(om.p.n_grids), divb_at=divb_at)
+    om.init_steps()
+    rm.init_steps()
+    _compare(om, rm, f"{cfg} after the time-step set-up")
+    return om, rm
+
+
+def _compare(om, rm, what):
+    got = rm.fields()
+    for q in range(34):
+        assert_same(om.cur[q], got[q], f"{what}: field {q}")
+    assert om.s.t == rm.get("t"), what
+    assert_same(om.t_stepnew, rm.array("t_stepnew"), f"{what}: t_stepnew")
+
+
+@pytest.mark.parametrize("cfg,nsteps", [("tiny", 1), ("tiny", 4), ("tiny3", 1), ("tiny3", 3)])
+def test_main_steps(cfg, nsteps):
+    om, rm = _pair(cfg, None)
+    start = om.cur.copy()
+    for _ in range(nsteps):
+        assert om.main_step() == 0
+    rm.steps(nsteps)
+    assert (~same_bits(rm.fields(), start)).sum() > 0.5 * start.size   # the state moved
+    _compare(om, rm, f"{cfg} after {nsteps} step(s)")
+
+
+@pytest.mark.parametrize("cfg,nsteps,divb_step", [("tiny", 1, 1), ("tiny3", 2, 2)])
+def test_main_steps_with_divb(cfg, nsteps, divb_step):
+    """The div B pass of the main step in which t reaches the fluid-file time."""
+    from g3m3_gb300.state import make_config
+    from oracle.oracle import OracleModel
+    probe = OracleModel(make_config(cfg))
+    probe.init_steps()
+    for _ in range(divb_step):
+        probe.main_step()
+    om, rm = _pair(cfg, divb_at=probe.s.t)
+    for n in range(1, nsteps + 1):
+        assert om.main_step() == 0
+        if n == divb_step:
+            om.divb_all()
+    rm.steps(nsteps)
+    _compare(om, rm, f"{cfg} after {nsteps} step(s), div B in step {divb_step}")
+
+
+def test_pin_detects_a_change():
+    """A one-ulp change in one cell of the reference's input shows up."""
+    om, rm = _pair("tiny3", None)
+    a = rm.array("hpresx")
+    a[1, 4, 6, 7] = np.nextafter(a[1, 4, 6, 7], np.float32(np.inf))
+    om.main_step()
+    rm.steps(1)
+    got = rm.fields()
+    assert any(not same_bits(om.cur[q], got[q]).all() for q in range(34))
+
+
+@pytest.mark.parametrize("cfg", ["tiny", "tiny3"])
+def test_reference_reproduces_committed_digests(cfg):
+    """The committed golden digests (tests/golden/oracle_digests.json, which
+    the library must reproduce on the GPU) are the reference's own results:
+    its set-up and main loop from the same seeded state give them."""
+    import json
+    import os
+    from _refmain import RefMain
+    from g3m3_gb300.state import make_config
+    from golden.make_golden import field_digests, input_digest
+    from oracle.oracle import OracleModel
+    here = os.path.dirname(os.path.abspath(__file__))
+    rec = json.load(open(os.path.join(here, "golden", "oracle_digests.json")))["cases"][cfg]
+    st = make_config(cfg)
+    assert input_digest(st) == rec["input"]
+    om = OracleModel(st)        # only for its starting copies: old = 0, wrk = cur
+    rm = RefMain(cfg)
+    rm.load_state(om.p, om.cur, om.old, om.wrk, om.b0, om.resistive, om.lists, 0.0, np.zeros(om.p.n_grids))
+    rm.init_steps()
+    done = 0
+    for n in sorted(int(k) for k in rec["steps"]):
+        rm.steps(n - done)
+        done = n
+        want = rec["steps"][str(n)]
+        assert field_digests(rm.fields()) == want["fields"], f"{cfg}: fields after {n} step(s)"
+        assert rm.get("t") == want["t"]
+        assert [float(x) for x in rm.array("t_stepnew")] == want["t_stepnew"]
