@@ -118,6 +118,10 @@ def statements(text):
     statement are skipped, as the standard allows)."""
     buf, start = "", None
     for n, raw in enumerate(text.splitlines(), 1):
+        d = raw.strip().lower()
+        if d.startswith("!$omp") and not buf:
+            yield n, "!$omp " + " ".join(d[5:].split())   # an OpenMP directive
+            continue
         s = _strip_comment(raw.replace("\t", " ")).strip()
         if not s:
             continue
@@ -499,6 +503,8 @@ def declaration(u, st, ln):
         return True
     if st.startswith("implicit "):
         raise TranslateError(f"{u.name}: IMPLICIT other than none is not supported")
+    if st.startswith("!$omp"):
+        return False           # a directive starts the executable part
     if st.startswith("!$") or st in ("save",):
         return True
     m = re.match(r"^dimension\s+(.*)$", st)
@@ -594,6 +600,7 @@ class Gen:
         self.loop = 0
         self.retyped = {}     # unit -> {dummy: type its callee reads it as}
         self.main = False     # translating the main program's loop
+        self.omp = False      # OpenMP directives become parallel loops
         for u in units:
             self.layout_commons(u)
 
@@ -1012,16 +1019,55 @@ class Gen:
         out.append(pad + "{ " + " ".join(pre) + f" ref_{name}(" + ", ".join(cargs) + "); "
                    + " ".join(post) + " }")
 
+    def omp_private(self, u, start):
+        """Scalars a parallel loop assigns (its temporaries and inner loop
+        indices): private to each thread, which is what the loop's
+        iterations being independent requires.  The reference's directives
+        name no clauses, so its own OpenMP build shares them and races."""
+        depth, names = 0, []
+        for ln, st in u.body[start:]:
+            if _DO_START.match(st):
+                depth += 1
+                m = re.match(r"^do\s+(\w+)\s*=", st)
+                if m and m.group(1) not in names:
+                    names.append(m.group(1))
+            elif _DO_END.match(st):
+                depth -= 1
+                if depth == 0:
+                    break
+            else:
+                tail = st
+                m = re.match(r"^if\s*\(", st)
+                if m:
+                    j = matching_paren(st, m.end() - 1)
+                    tail = st[j + 1:].strip()
+                m = re.match(r"^(\w+)\s*=(?!=)", tail)
+                if m and m.group(1) not in names:
+                    names.append(m.group(1))
+        out = []
+        for n in names[1:] if names else []:
+            sym = u.syms.get(n)
+            if sym is not None and sym.dims is not None:
+                continue
+            if sym is not None and (sym.is_dummy or sym.common is not None):
+                raise TranslateError(f"{u.name}: parallel loop assigns the shared scalar {n}")
+            self.locals_used.add(n)
+            out.append(self.cn(n))
+        return out
+
     def body(self, u):
         out = []
         ind = 1
         stack = []
-        for ln, st in u.body:
+        pending_omp = False
+        for idx, (ln, st) in enumerate(u.body):
             self.where = (u.src, ln, st)
             pad = "  " * ind
             out.append(f"{pad}/* {u.src}:{ln} */")
             if st.startswith("!$"):
+                pending_omp = st.startswith("!$omp parallel do")
                 continue
+            omp_here, pending_omp = pending_omp, False
             m = re.match(r"^(\d+)\s+(.*)$", st)
             if m:
                 raise TranslateError(f"{u.src}:{ln}: labels are not supported")
@@ -1043,6 +1089,22 @@ class Gen:
                 vc, vt = self.name_ref(var)
                 self.loop += 1
                 L = self.loop
+                if omp_here and self.omp and len(parts) > 2:
+                    try:
+                        self.eval_const(u, parse_expr(parts[2]))
+                    except TranslateError:
+                        omp_here = False      # a step known only at run time: kept serial
+                if omp_here and self.omp:
+                    priv = self.omp_private(u, idx)
+                    clause = f" private({', '.join(priv)})" if priv else ""
+                    out.append(f"{pad}{{ const int lo_{L} = {lo}, hi_{L} = {hi};")
+                    sv = int(self.eval_const(u, parse_expr(parts[2]))) if len(parts) > 2 else 1
+                    cmp = "<=" if sv > 0 else ">="
+                    out.append(f"{pad}  _Pragma(\"omp parallel for schedule(static){clause}\")")
+                    out.append(f"{pad}  for ({vc} = lo_{L}; {vc} {cmp} hi_{L}; {vc} += {sv}) {{")
+                    stack.append("dofor")
+                    ind += 1
+                    continue
                 # trip count fixed at entry, as Fortran defines it
                 out.append(f"{pad}{{ const int lo_{L} = {lo}, hi_{L} = {hi}, st_{L} = {step};")
                 out.append(f"{pad}  long tc_{L} = ((long)hi_{L} - lo_{L} + st_{L}) / st_{L};")
@@ -1493,17 +1555,27 @@ def translate(code_dir, out_dir=OUT):
 MAIN_CONFIGS = {
     "tiny": {"limit": "8.", "n_grids": "1", "mbndry": "1"},
     "tiny3": {"limit": "8.", "n_grids": "3", "mbndry": "1"},
+    "nested": {},            # the reference's own: limit 60 (121x121x61), 5 boxes
 }
+# (grid, OpenMP): the serial builds are the parity reference; the OpenMP
+# builds time the reference on all host cores (tiny3 is checked against its
+# serial build bit for bit)
+MAIN_BUILDS = [("tiny", False), ("tiny3", False), ("tiny3", True), ("nested", True)]
 
 
-def translate_main(code_dir, tag, overrides, out_dir=OUT):
+def main_stem(tag, omp):
+    return f"g3m3_ref_main_{tag}" + ("_omp" if omp else "")
+
+
+def translate_main(code_dir, tag, overrides, out_dir=OUT, omp=False):
     """All routines plus the main program's time loop for one grid size:
-    g3m3_ref_main_<tag>.c and its variable list g3m3_ref_main_<tag>.json."""
+    <stem>.c and its variable list <stem>.json (stem from main_stem)."""
     units = []
     for f in FILES:
         units += parse_units(os.path.join(code_dir, f + ".f90"))
     prog = parse_main_loop(os.path.join(code_dir, "3d_main.f90"), code_dir, overrides)
     g = Gen(units)
+    g.omp = omp
     g.layout_commons(prog)
     order = [u.name for u in units]
     g.where = None
@@ -1513,13 +1585,14 @@ def translate_main(code_dir, tag, overrides, out_dir=OUT):
     except (TranslateError, KeyError, ValueError, IndexError, StopIteration) as e:
         raise TranslateError(f"at {g.where}: {type(e).__name__}: {e}") from e
     os.makedirs(out_dir, exist_ok=True)
-    cpath = os.path.join(out_dir, f"g3m3_ref_main_{tag}.c")
+    stem = main_stem(tag, omp)
+    cpath = os.path.join(out_dir, stem + ".c")
     with open(cpath, "w") as fh:
         fh.write("\n".join(src + main_src) + "\n")
     meta = g.meta(order)
-    meta["main"] = {"variables": main_meta, "overrides": overrides,
+    meta["main"] = {"variables": main_meta, "overrides": overrides, "openmp": omp,
                     "loop_lines": list(prog.loop_lines), "init_lines": list(prog.init_lines)}
-    with open(os.path.join(out_dir, f"g3m3_ref_main_{tag}.json"), "w") as fh:
+    with open(os.path.join(out_dir, stem + ".json"), "w") as fh:
         json.dump(meta, fh, indent=1)
     return cpath
 
@@ -1527,13 +1600,14 @@ def translate_main(code_dir, tag, overrides, out_dir=OUT):
 def compile_ref(out_dir=OUT, cc="gcc", stem="g3m3_ref"):
     cpath = os.path.join(out_dir, stem + ".c")
     so = os.path.join(out_dir, "lib" + stem + ".so")
+    omp = ["-fopenmp"] if stem.endswith("_omp") else []
     # warnings are not shown, but the ones that reveal a mistranslated
     # argument (a pointer where a value belongs, or the reverse) are errors
-    r = subprocess.run([cc, "-O2", "-fPIC", "-shared", "-std=gnu11", "-ffp-contract=off",
+    r = subprocess.run([cc] + omp + ["-O2", "-fPIC", "-shared", "-std=gnu11", "-ffp-contract=off",
                         "-fno-fast-math", "-fwrapv", "-Werror=int-conversion",
                         "-Werror=incompatible-pointer-types", "-Werror=implicit-function-declaration",
                         "-Werror=pointer-to-int-cast", "-Werror=int-to-pointer-cast",
-                        "-o", so, cpath, "-lm"], capture_output=True, text=True)
+                        "-Wl,-Bsymbolic", "-o", so, cpath, "-lm"], capture_output=True, text=True)
     if r.returncode:
         errs = [ln for ln in r.stderr.splitlines() if "error" in ln]
         raise TranslateError(f"{cpath} does not compile:\n" + "\n".join(errs[:20]))
@@ -1547,11 +1621,11 @@ def reference_code_dir():
 
 def main(argv):
     code_dir = argv[1] if len(argv) > 1 else reference_code_dir()
-    stems = ["g3m3_ref"] + [f"g3m3_ref_main_{t}" for t in MAIN_CONFIGS]
+    stems = ["g3m3_ref"] + [main_stem(t, o) for t, o in MAIN_BUILDS]
     if os.path.isdir(code_dir):
         translate(code_dir)
-        for tag, ov in MAIN_CONFIGS.items():
-            translate_main(code_dir, tag, ov)
+        for tag, omp in MAIN_BUILDS:
+            translate_main(code_dir, tag, MAIN_CONFIGS[tag], omp=omp)
     from concurrent.futures import ThreadPoolExecutor
     todo = [st for st in stems if os.path.exists(os.path.join(OUT, st + ".c"))]
     # sources translated elsewhere may have travelled here without the reference

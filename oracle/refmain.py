@@ -1,7 +1,10 @@
-"""ctypes access to oracle/_ref/libg3m3_ref_main_<tag>.so: the reference's
-main time loop (the body of ``do while(t.lt.tmax)``, code/3d_main.f90),
-translated to C with all its routines by oracle/fortran_to_c.py for one grid
-size.  TEST INFRASTRUCTURE ONLY.
+"""ctypes access to oracle/_ref/libg3m3_ref_main_<tag>[_omp].so: the
+reference's time-step set-up and main time loop (the body of ``do
+while(t.lt.tmax)``, code/3d_main.f90), translated to C with all its routines
+by oracle/fortran_to_c.py for one grid size.
+
+TEST INFRASTRUCTURE ONLY: the tests use it as the parity reference of the
+main step, and bench.py's CPU legs time it as the reference's own CPU path.
 
 The main program's variables are globals ``ref_main_<name>``; this module
 loads a state into them the way the reference's initialisation leaves it,
@@ -17,7 +20,7 @@ import os
 
 import numpy as np
 
-from _refpin import REF, load as load_routines
+from oracle.fortran_to_c import OUT as REF, main as _build_all
 from g3m3_gb300.params import FIELD_NAMES
 
 _CT = {"int": ctypes.c_int32, "logical": ctypes.c_int32, "float": ctypes.c_float,
@@ -27,14 +30,15 @@ BIG = 1.0e30
 
 
 class RefMain:
-    def __init__(self, tag):
-        so = os.path.join(REF, f"libg3m3_ref_main_{tag}.so")
+    def __init__(self, tag, omp=False):
+        stem = f"g3m3_ref_main_{tag}" + ("_omp" if omp else "")
+        so = os.path.join(REF, f"lib{stem}.so")
         if not os.path.exists(so):
-            load_routines()          # builds everything where the sources exist
+            _build_all(["fortran_to_c"])     # builds everything where the sources exist
         if not os.path.exists(so):
             raise FileNotFoundError(so)
         self.lib = ctypes.CDLL(so)
-        with open(os.path.join(REF, f"g3m3_ref_main_{tag}.json")) as fh:
+        with open(os.path.join(REF, f"{stem}.json")) as fh:
             self.meta = json.load(fh)
         self.vars = self.meta["main"]["variables"]
         self.keep = []
@@ -154,6 +158,13 @@ class RefMain:
             self.set(ts1=float(divb_at), tsave=BIG, divb_lores=1, fluid_f=11, offset_f=0)
         self.set(t=float(t))
         self.array("t_stepnew")[...] = np.asarray(t_stepnew, np.float64)
+
+    def box_steps(self):
+        """Box-steps of box 1..n_grids in the last main step: box b steps
+        every t_step(b) through the main step of length t_step(n_grids)
+        (3d_main.f90:1954-1966)."""
+        ts = self.array("t_step")
+        return [int(round(ts[-1] / ts[b])) for b in range(len(ts))]
 
     def fields(self):
         return np.stack([self.array(n) for n in FIELD_NAMES])

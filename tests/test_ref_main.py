@@ -22,7 +22,7 @@ pytestmark = pytest.mark.skipif(_refpin.load() is None,
 def _pair(cfg, divb_at):
     """The seeded state in both, after each side's time-step set-up (which
     must agree too)."""
-    from _refmain import RefMain
+    from oracle.refmain import RefMain
     from g3m3_gb300.state import make_config
     from oracle.oracle import OracleModel
     om = OracleModel(make_config(cfg))
@@ -47,9 +47,13 @@ def _compare(om, rm, what):
 def test_main_steps(cfg, nsteps):
     om, rm = _pair(cfg, None)
     start = om.cur.copy()
+    cells = om.p.nx * om.p.ny * om.p.nz
     for _ in range(nsteps):
+        cu = om.cell_updates
         assert om.main_step() == 0
-    rm.steps(nsteps)
+        rm.steps(1)
+        # the cell-update count the benchmark derives from the reference's schedule
+        assert sum(rm.box_steps()) * cells == om.cell_updates - cu
     assert (~same_bits(rm.fields(), start)).sum() > 0.5 * start.size   # the state moved
     _compare(om, rm, f"{cfg} after {nsteps} step(s)")
 
@@ -90,7 +94,7 @@ def test_reference_reproduces_committed_digests(cfg):
     its set-up and main loop from the same seeded state give them."""
     import json
     import os
-    from _refmain import RefMain
+    from oracle.refmain import RefMain
     from g3m3_gb300.state import make_config
     from golden.make_golden import field_digests, input_digest
     from oracle.oracle import OracleModel
@@ -110,3 +114,36 @@ def test_reference_reproduces_committed_digests(cfg):
         assert field_digests(rm.fields()) == want["fields"], f"{cfg}: fields after {n} step(s)"
         assert rm.get("t") == want["t"]
         assert [float(x) for x in rm.array("t_stepnew")] == want["t_stepnew"]
+
+
+def test_openmp_build_matches_serial():
+    """The reference's OpenMP loops, with the temporaries of each parallel
+    loop private (its iterations are independent), give the serial
+    reference's bits; this build times the reference on all host cores."""
+    import os
+    import subprocess
+    import sys
+    code = r'''
+import sys, numpy as np
+sys.path[:0] = [sys.argv[2], sys.argv[1]]
+from oracle.refmain import RefMain
+from g3m3_gb300.state import make_config
+from oracle.oracle import OracleModel
+om = OracleModel(make_config("tiny3"))
+out = []
+for omp in (False, True):
+    rm = RefMain("tiny3", omp=omp)
+    rm.load_state(om.p, om.cur, om.old, om.wrk, om.b0, om.resistive, om.lists, 0.0, np.zeros(3))
+    rm.init_steps()
+    rm.steps(2)
+    out.append(rm.fields().copy())
+a, b = out
+same = (a == b) | (np.isnan(a) & np.isnan(b))
+print("SAME" if same.all() else "DIFF %d" % (~same).sum())
+'''
+    here = os.path.dirname(os.path.abspath(__file__))
+    env = dict(os.environ, OMP_NUM_THREADS="4")
+    r = subprocess.run([sys.executable, "-c", code, here, os.path.dirname(here)], env=env,
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert r.stdout.strip().endswith("SAME"), r.stdout[-500:]
