@@ -1555,12 +1555,13 @@ def translate(code_dir, out_dir=OUT):
 MAIN_CONFIGS = {
     "tiny": {"limit": "8.", "n_grids": "1", "mbndry": "1"},
     "tiny3": {"limit": "8.", "n_grids": "3", "mbndry": "1"},
+    "small": {"limit": "30.", "n_grids": "1", "mbndry": "1"},   # one box 61x61x31
     "nested": {},            # the reference's own: limit 60 (121x121x61), 5 boxes
 }
 # (grid, OpenMP): the serial builds are the parity reference; the OpenMP
-# builds time the reference on all host cores (tiny3 is checked against its
-# serial build bit for bit)
-MAIN_BUILDS = [("tiny", False), ("tiny3", False), ("tiny3", True), ("nested", True)]
+# builds time the reference on all host cores and make the production-size
+# digests (tiny3 is checked against its serial build bit for bit)
+MAIN_BUILDS = [("tiny", False), ("tiny3", False), ("small", False), ("tiny3", True), ("nested", True)]
 
 
 def main_stem(tag, omp):

@@ -1,5 +1,7 @@
 """Writes tests/golden/ref_digests.json: SHA-256 digests of the reference's
-own results for every per-routine case of tests/_refcases.py.
+own results for every per-routine case of tests/_refcases.py, and of its
+main loop on the one-box 61x61x31 grid (20 main steps) and the production
+nested grid (5 boxes of 121x121x61, one main step).
 
 The results come from the reference's Fortran routines translated to C and
 compiled by oracle/fortran_to_c.py (oracle/_ref/libg3m3_ref.so), so this
@@ -42,6 +44,46 @@ def digests(results):
     return {k: digest(np.asarray(v)) for k, v in sorted(results.items())}
 
 
+# main-loop cases: (name, grid, build with OpenMP, digest after these main
+# steps) -- BASELINE's one-box 61x61x31 grid for 20 steps and the production
+# nested grid (5 boxes of 121x121x61) for one main step, no div B pass
+MAIN_CASES = [("small", "small", False, [1, 5, 20]), ("nested", "nested", True, [1])]
+
+
+def main_start(name):
+    """The seeded state with the starting copies every side uses: old = 0,
+    wrk = cur."""
+    from g3m3_gb300.state import make_config
+    st = make_config(name, divb_every=0)
+    return st, np.zeros_like(st.cur), st.cur.copy()
+
+
+def main_record(fields, t, t_stepnew, cell_updates):
+    return {"fields": [digest(f) for f in fields], "t": float(t),
+            "t_stepnew": [float(x) for x in t_stepnew], "cell_updates": int(cell_updates)}
+
+
+def make_main():
+    from oracle.refmain import RefMain
+    out = {}
+    for name, grid, omp, steps in MAIN_CASES:
+        st, old, wrk = main_start(name)
+        p = st.params
+        rm = RefMain(grid, omp=omp)
+        rm.load_state(p, st.cur, old, wrk, st.b0, st.resistive, st.lists, 0.0, np.zeros(p.n_grids))
+        rm.init_steps()
+        cells = p.nx * p.ny * p.nz
+        rec, done, cu = {}, 0, 0
+        for n in steps:
+            while done < n:
+                rm.steps(1)
+                cu += sum(rm.box_steps()) * cells
+                done += 1
+            rec[str(n)] = main_record(rm.fields(), rm.get("t"), rm.array("t_stepnew"), cu)
+        out[name] = rec
+    return out
+
+
 def make():
     import _refpin
     from _refcases import CASES, run
@@ -55,6 +97,7 @@ def make():
            "cases": {}}
     for cid, fn, kw, _ in CASES:
         out["cases"][cid] = digests(run(cid, "ref"))
+    out["main"] = make_main()
     with open(OUT, "w") as fh:
         json.dump(out, fh, indent=0, sort_keys=True)
         fh.write("\n")
