@@ -372,6 +372,11 @@ def matching_paren(s, i):
 # Symbols
 # --------------------------------------------------------------------------
 
+# the C type of default REAL: float, or double for the reference's FP64 build
+# (what -fdefault-real-8 gives: default REAL variables and literals in
+# double precision; REAL(dp) stays double)
+REAL = {"t": "float"}
+
 CTYPE = {"int": "int", "float": "float", "double": "double", "logical": "int",
          "char": "char"}
 RANK = {"logical": 0, "int": 1, "float": 2, "double": 3}
@@ -423,7 +428,7 @@ class Unit:
             return s.type
         if self.implicit_none:
             raise TranslateError(f"{self.name}: {name} has no type under implicit none")
-        return "int" if name[0] in "ijklmn" else "float"
+        return "int" if name[0] in "ijklmn" else REAL["t"]
 
 
 _DECL = re.compile(r"^(integer|real|double\s*precision|logical|character)\b(.*)$")
@@ -469,7 +474,7 @@ def _kind_type(base, spec):
     if spec in ("(dp)", "(kind=dp)", "*8", "(8)", "(kind=8)"):
         return "double"
     if spec in ("", "*4", "(4)", "(kind=4)"):
-        return "float"
+        return REAL["t"]
     raise TranslateError(f"unsupported real kind {spec!r}")
 
 
@@ -679,6 +684,8 @@ class Gen:
             if txt.startswith("."):
                 txt = "0" + txt
             txt = re.sub(r"\.(e|$)", r".0\1", txt)
+            if REAL["t"] == "double":
+                return f"{txt}", "double"
             return (f"{txt}", "double") if dbl else (f"{txt}f", "float")
         if k == "logic":
             return ("1" if e[1] else "0"), "logical"
@@ -730,7 +737,7 @@ class Gen:
             return f"{fn}({b}, {e})", tb
         t = tb if RANK[tb] >= RANK[te] else te
         if t == "int":
-            t = "float"
+            t = REAL["t"]
         fn = "powf" if t == "float" else "pow"
         return f"{fn}({b}, {e})", t
 
@@ -797,7 +804,7 @@ class Gen:
         if n in ("max", "min", "amax1", "amin1", "max0", "min0", "dmax1", "dmin1"):
             t = max(types, key=lambda x: RANK[x])
             if n in ("amax1", "amin1"):
-                t = "float"
+                t = REAL["t"]
             fn = f"ref_{'max' if 'max' in n else 'min'}_{CTYPE[t]}"
             acc = f"(({CTYPE[t]}){codes[0]})"
             for c in codes[1:]:
@@ -821,7 +828,7 @@ class Gen:
             t = types[0]
             return f"{'atan2f' if t == 'float' else 'atan2'}({codes[0]}, {codes[1]})", t
         if n in ("float", "real", "sngl"):
-            if len(args) == 2:
+            if len(args) == 2 or REAL["t"] == "double":
                 return f"((double)({codes[0]}))", "double"
             return f"((float)({codes[0]}))", "float"
         if n == "dble":
@@ -1346,7 +1353,7 @@ class Gen:
         u.body = loop_body
         for n in self.locals_used:
             u.sym(n)
-        glob, prolog, meta = [], [], {}
+        glob, prolog, meta, allocs = [], [], {}, []
         for name, sym in sorted(u.syms.items()):
             if (sym.param is not None and sym.dims is None) or name.startswith("s_"):
                 continue
@@ -1398,13 +1405,18 @@ class Gen:
                 n = 1
                 for e in ext:
                     n *= e
-                # a guard of zeros on both sides: the loop reads t_old(0)
-                # and t_new(0) (box - 1 with box = 1)
-                glob.append(f"{ct} {g}_mem[{n + 16}] __attribute__((aligned(16)));")
-                glob.append(f"{ct}* const {g} = {g}_mem + 8;")
+                # on the heap (the production grid's arrays exceed what a
+                # shared library's static data may hold), with a guard of
+                # zeros on both sides: the loop reads t_old(0) and t_new(0)
+                # (box - 1 with box = 1)
+                glob.append(f"{ct}* {g} = 0;")
+                allocs.append(f"  {g} = ({ct}*)calloc({n + 16}, sizeof({ct})) + 8;")
                 meta[name] = {"type": t, "dims": ext}
         out = [f"/* ---- {u.src}: the body of the time loop, lines {u.loop_lines[0]}-{u.loop_lines[1]} ---- */"]
         out += glob
+        out.append("__attribute__((constructor)) static void ref_main_alloc(void) {")
+        out += allocs
+        out.append("}")
         out.append(f"/* the time-step set-up before the loop, lines {u.init_lines[0]}-{u.init_lines[1]} */")
         out.append("void ref_main_init_steps(void) {")
         out += prolog
@@ -1562,15 +1574,26 @@ MAIN_CONFIGS = {
 # builds time the reference on all host cores and make the production-size
 # digests (tiny3 is checked against its serial build bit for bit)
 MAIN_BUILDS = [("tiny", False), ("tiny3", False), ("small", False), ("tiny3", True), ("nested", True)]
+# the reference in FP64 (default REAL as double), to state the FP32 error:
+# (grid, OpenMP)
+R8_BUILDS = [("tiny3", False), ("small", False), ("nested", True)]
 
 
-def main_stem(tag, omp):
-    return f"g3m3_ref_main_{tag}" + ("_omp" if omp else "")
+def main_stem(tag, omp, real8=False):
+    return f"g3m3_ref_main_{tag}" + ("_r8" if real8 else "") + ("_omp" if omp else "")
 
 
-def translate_main(code_dir, tag, overrides, out_dir=OUT, omp=False):
+def translate_main(code_dir, tag, overrides, out_dir=OUT, omp=False, real8=False):
     """All routines plus the main program's time loop for one grid size:
     <stem>.c and its variable list <stem>.json (stem from main_stem)."""
+    REAL["t"] = "double" if real8 else "float"
+    try:
+        return _translate_main(code_dir, tag, overrides, out_dir, omp, real8)
+    finally:
+        REAL["t"] = "float"
+
+
+def _translate_main(code_dir, tag, overrides, out_dir, omp, real8):
     units = []
     for f in FILES:
         units += parse_units(os.path.join(code_dir, f + ".f90"))
@@ -1586,7 +1609,7 @@ def translate_main(code_dir, tag, overrides, out_dir=OUT, omp=False):
     except (TranslateError, KeyError, ValueError, IndexError, StopIteration) as e:
         raise TranslateError(f"at {g.where}: {type(e).__name__}: {e}") from e
     os.makedirs(out_dir, exist_ok=True)
-    stem = main_stem(tag, omp)
+    stem = main_stem(tag, omp, real8)
     cpath = os.path.join(out_dir, stem + ".c")
     with open(cpath, "w") as fh:
         fh.write("\n".join(src + main_src) + "\n")
@@ -1622,11 +1645,14 @@ def reference_code_dir():
 
 def main(argv):
     code_dir = argv[1] if len(argv) > 1 else reference_code_dir()
-    stems = ["g3m3_ref"] + [main_stem(t, o) for t, o in MAIN_BUILDS]
+    stems = (["g3m3_ref"] + [main_stem(t, o) for t, o in MAIN_BUILDS]
+             + [main_stem(t, o, True) for t, o in R8_BUILDS])
     if os.path.isdir(code_dir):
         translate(code_dir)
         for tag, omp in MAIN_BUILDS:
             translate_main(code_dir, tag, MAIN_CONFIGS[tag], omp=omp)
+        for tag, omp in R8_BUILDS:
+            translate_main(code_dir, tag, MAIN_CONFIGS[tag], omp=omp, real8=True)
     from concurrent.futures import ThreadPoolExecutor
     todo = [st for st in stems if os.path.exists(os.path.join(OUT, st + ".c"))]
     # sources translated elsewhere may have travelled here without the reference

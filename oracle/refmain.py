@@ -30,8 +30,8 @@ BIG = 1.0e30
 
 
 class RefMain:
-    def __init__(self, tag, omp=False):
-        stem = f"g3m3_ref_main_{tag}" + ("_omp" if omp else "")
+    def __init__(self, tag, omp=False, real8=False):
+        stem = f"g3m3_ref_main_{tag}" + ("_r8" if real8 else "") + ("_omp" if omp else "")
         so = os.path.join(REF, f"lib{stem}.so")
         if not os.path.exists(so):
             _build_all(["fortran_to_c"])     # builds everything where the sources exist
