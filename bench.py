@@ -277,6 +277,7 @@ def run_batched(args, device, members=16):
     ens = Ensemble(ctx, states)
     cells = sorted({(st.params.nx, st.params.ny, st.params.nz) for st in states}, reverse=True)
     del states
+    tuned = ens.autotune()
     ens.init_steps()
     stream = torch.cuda.ExternalStream(ens.stream)
 
@@ -308,6 +309,7 @@ def run_batched(args, device, members=16):
                         + ", ".join(f"{a}x{b}x{c}" for a, b, c in cells) + " cycling; upstream n, |v|, IMF "
                         "clock angle and |B| drawn from the seed",
             "members": members,
+            "autotuned_fcsmooth": {f"{a}x{b}x{c}": v for (a, b, c), v in tuned.items()},
             "graph": {"value": vg, "unit": "cell-updates/s", "ms_per_step": ms_g / args.steps, "steps": args.steps,
                       "gpu_launches": int(k_g), "mode": "one CUDA graph per main step for all members, "
                       "members on their own streams"},

@@ -295,6 +295,19 @@ class Ensemble:
         for m in self.members:
             m.init_steps()
 
+    def autotune(self):
+        """Picks the flux-correction form once per distinct box size (on the
+        first member of that size) and gives it to every member of the size;
+        returns {(nx, ny, nz): variant}."""
+        chosen = {}
+        for m in self.members:
+            key = (m.p.nx, m.p.ny, m.p.nz)
+            if key not in chosen:
+                chosen[key] = m.autotune()
+            else:
+                m.set_variant(1, chosen[key])
+        return chosen
+
     def run(self, nsteps: int, graph: bool = True, concurrent: bool = False):
         """graph: one CUDA graph per main step for all members; concurrent
         (without graph): every member launched at once on its own stream;

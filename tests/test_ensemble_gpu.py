@@ -82,3 +82,27 @@ def test_ensemble_divb_inside_steps(mode):
             assert_same(out[q], om.cur[q], f"member {i} field {q}")
         for q in (31, 32, 33):
             assert rel_l2(out[q] - before[q], om.cur[q] - before[q]) < 0.2
+
+
+def test_ensemble_autotune_per_box_size():
+    """One flux-correction form chosen per distinct box size and shared by
+    the members of that size; the members still give the oracle's bits."""
+    from g3m3_gb300.api import Context, Ensemble
+    from oracle.oracle import OracleModel
+    from g3m3_gb300.state import ensemble_member
+    states = [ensemble_member(i, n_grids=2, limits=LIMITS) for i in range(4)]   # sizes 17, 21, 25, 17
+    with Context() as ctx:
+        ens = Ensemble(ctx, states)
+        chosen = ens.autotune()
+        assert sorted(chosen) == sorted({(s.params.nx, s.params.ny, s.params.nz) for s in states})
+        assert all(v in range(7) for v in chosen.values())
+        ens.init_steps()
+        ens.run(2, graph=True)
+        outs = [m.state() for m in ens.members]
+    for st, g in zip(states, outs):
+        om = OracleModel(st, omp=True)
+        om.init_steps()
+        for _ in range(2):
+            assert om.main_step() == 0
+        for q in range(34):
+            assert_same(g[q], om.cur[q], f"member field {q}")
