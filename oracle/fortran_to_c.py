@@ -907,8 +907,6 @@ class Gen:
                 return ("pow", subst(e[1]), subst(e[2]))
             return e
 
-        lhs = ("ref", name, [("name", f"s_{i}") if sub[0] == "slice" else sub
-                             for i, sub in zip(range(len(subs)), subs)])
         # number the slice loop variables in order of the slices
         kk, na = 0, []
         for sub in subs:
@@ -922,7 +920,6 @@ class Gen:
         for i in range(rank):
             self.u.sym(f"s_{i}").type = "int"
         # outermost loop over the last sliced dimension (column-major order)
-        pad = "  " * ind
         body_ind = ind
         opened = 0
         for i in range(rank - 1, -1, -1):
@@ -937,7 +934,6 @@ class Gen:
         for i in range(opened):
             body_ind -= 1
             out.append(f"{'  ' * body_ind}}}")
-        del pad
 
     def section_temp(self, e, ct, pre, post):
         """An array section as an actual argument: a contiguous copy made
@@ -960,7 +956,7 @@ class Gen:
         elem, _ = self.ref(name, na)
         size = " * ".join(f"{cb}_ex{d}" for d, _ in vars_)
         pre.append(f"{ct}* {tmp} = ({ct}*)malloc(sizeof({ct}) * (size_t)({size})); long n_{tmp} = 0;")
-        loops_open, loops_close = "", ""
+        loops_open = ""
         for d, v in reversed(vars_):
             loops_open += f"for (int {v} = (int){cb}_lo{d}; {v} < (int)({cb}_lo{d} + {cb}_ex{d}); {v}++) "
         pre.append(loops_open + f"{tmp}[n_{tmp}++] = {elem};")
@@ -1032,7 +1028,7 @@ class Gen:
         iterations being independent requires.  The reference's directives
         name no clauses, so its own OpenMP build shares them and races."""
         depth, names = 0, []
-        for ln, st in u.body[start:]:
+        for _, st in u.body[start:]:
             if _DO_START.match(st):
                 depth += 1
                 m = re.match(r"^do\s+(\w+)\s*=", st)
@@ -1093,7 +1089,7 @@ class Gen:
                 lo, _ = self.ex(parse_expr(parts[0]))
                 hi, _ = self.ex(parse_expr(parts[1]))
                 step = self.ex(parse_expr(parts[2]))[0] if len(parts) > 2 else "1"
-                vc, vt = self.name_ref(var)
+                vc, _ = self.name_ref(var)
                 self.loop += 1
                 L = self.loop
                 if omp_here and self.omp and len(parts) > 2:
@@ -1220,7 +1216,7 @@ class Gen:
         if isinstance(tc, tuple):
             self.section_assign(tc, rhs_s, out, ind)
             return
-        rc, rt = self.ex(parse_expr(rhs_s))
+        rc, _ = self.ex(parse_expr(rhs_s))
         out.append(f"{pad}{tc} = ({CTYPE[tt]})({rc});")
 
     # ---- one subroutine ----
@@ -1229,10 +1225,9 @@ class Gen:
         params = []
         for a in u.args:
             t = u.type_of(a)
-            params.append(f"{CTYPE[t]}* restrict {a}" if False else f"{CTYPE[t]}* {a}")
+            params.append(f"{CTYPE[t]}* {a}")
         head = f"void ref_{u.name}({', '.join(params) if params else 'void'})"
         decl, setup, free = [], [], []
-        saved_reset = []
         self.locals_used = set()
         body = self.body(u)
         for n in self.locals_used:
@@ -1248,7 +1243,6 @@ class Gen:
             if s.dims is None:
                 init = self.ex(pexpr(s.init))[0] if s.init is not None else "0"
                 decl.append(f"  static {ct} {name} = {init};")
-                saved_reset.append(f"{name}_reset")
                 continue
             try:
                 n = 1
@@ -1273,7 +1267,7 @@ class Gen:
                 else:
                     hc = self.ex(hi)[0]
                     lines.append(f"  const long {name}_ex{d} = (long)({hc}) - {name}_lo{d} + 1;")
-        for kind, name, ct in setup:
+        for _, name, ct in setup:
             s = u.syms[name]
             ext = " * ".join(f"{name}_ex{d}" for d in range(len(s.dims)))
             lines.append(f"  {ct}* {name} = ({ct}*)calloc((size_t)({ext}) > 0 ? (size_t)({ext}) : 1, sizeof({ct}));")
@@ -1285,7 +1279,7 @@ class Gen:
         out.append("L_return:;")
         out += free
         out.append("}")
-        return out, [d for d in decl]
+        return out
 
     def module(self, order):
         out = [
@@ -1333,11 +1327,8 @@ class Gen:
             u = self.units[name]
             params = [f"{CTYPE[u.type_of(a)]}* {a}" for a in u.args]
             out.append(f"void ref_{name}({', '.join(params) if params else 'void'});")
-        resets = []
         for name in order:
-            code, decls = self.unit(self.units[name])
-            out += code
-        del resets
+            out += self.unit(self.units[name])
         return out
 
     def main_unit(self, u):
@@ -1485,7 +1476,7 @@ def parse_main_loop(path, module_dir, overrides):
     become C globals.  `overrides` replaces PARAMETER values (grid size)."""
     text = open(path, encoding="latin-1").read()
     sts = list(statements(text))
-    ln0, st0 = sts[0]
+    st0 = sts[0][1]
     m = re.match(r"^program\s+(\w+)$", st0)
     if not m:
         raise TranslateError(f"{path}: does not start with PROGRAM")
