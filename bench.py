@@ -165,6 +165,7 @@ def run_ours(args):
     # the div B step (every 10th); the timed region runs the faster mode
     done = 0
     m.run(max(args.warmup, 3), graph=True)
+    m.divb_all()          # warm-up of the div B pass too (captures its iteration graphs)
     m.run(1, graph=False)
     done += max(args.warmup, 3) + 1
     TRIAL = 4
@@ -294,6 +295,8 @@ def run_batched(args, device, members=16):
         return e0.elapsed_time(e1), cu1 - cu0, k
 
     ens.run(max(args.warmup, 2), graph=True)   # captures the step graphs
+    for mm in ens.members:                     # and the div B iteration graphs
+        mm.divb_all()
     ens.run(2, graph=True, concurrent=True)    # and every member's own graphs
     ens.run(1, graph=False, concurrent=True)
     ms_g, cu_g, k_g = timed(args.steps, "graph")

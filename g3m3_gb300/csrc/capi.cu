@@ -133,6 +133,12 @@ int ensure_cg_scratch(g3m3_ctx* c, size_t cells) {
 // cg_step waits for that read-back and queues what the status asks for
 // (the next chunk, a restart, or nothing when the solve has ended), so a
 // caller can keep several solves on separate streams in flight.
+static cudaError_t launch_iterations(CgRun& r) {
+  if (r.graphs) return r.graphs->iterations(r.a, r.chunk, r.s);
+  divb_launch_iterations(r.a, r.chunk, r.s);
+  return cudaSuccess;
+}
+
 int cg_begin(g3m3_ctx* c, CgRun& r, float errlim, bool given, int redos0, int hint) {
   const size_t n = r.a.d.cells();
   CgState init{};
@@ -152,7 +158,7 @@ int cg_begin(g3m3_ctx* c, CgRun& r, float errlim, bool given, int redos0, int hi
   r.chunk = hint > 0 ? hint : 8;
   r.first = true;
   r.status = CG_RUNNING;
-  divb_launch_iterations(r.a, r.chunk, r.s);
+  G3M3_CUDA(c, launch_iterations(r));
   G3M3_CUDA(c, cudaMemcpyAsync(r.host_st, r.a.st, sizeof(CgState), cudaMemcpyDeviceToHost, r.s));
   return G3M3_OK;
 }
@@ -185,7 +191,7 @@ int cg_step(g3m3_ctx* c, CgRun& r, bool* done) {
     G3M3_CUDA(c, cudaGetLastError());
     return G3M3_OK;
   }
-  divb_launch_iterations(r.a, r.chunk, r.s);
+  G3M3_CUDA(c, launch_iterations(r));
   G3M3_CUDA(c, cudaMemcpyAsync(r.host_st, r.a.st, sizeof(CgState), cudaMemcpyDeviceToHost, r.s));
   return G3M3_OK;
 }
@@ -196,9 +202,9 @@ int cg_step(g3m3_ctx* c, CgRun& r, bool* done) {
 // device, restart after a growing residual (the reference's recursive call,
 // :112-125) until the SAVEd restart count reaches 3.
 int run_cg(g3m3_ctx* c, const DivbArgs& a, float errlim, bool given, int redos0, CgState* host_st,
-           cudaStream_t s, int* iters_out, float* residual2_out, int* status_out) {
+           cudaStream_t s, int* iters_out, float* residual2_out, int* status_out, CgGraphs* graphs = nullptr) {
   CgRun r;
-  r.a = a; r.host_st = host_st; r.s = s;
+  r.a = a; r.host_st = host_st; r.s = s; r.graphs = graphs;
   int rc = cg_begin(c, r, errlim, given, redos0, c->cg_hint);
   bool done = false;
   while (rc == G3M3_OK && !done) rc = cg_step(c, r, &done);
@@ -210,8 +216,11 @@ int run_cg(g3m3_ctx* c, const DivbArgs& a, float errlim, bool given, int redos0,
   return G3M3_OK;
 }
 
-int run_divb(g3m3_ctx* c, float* bx, float* by, float* bz, const Dims& d, float rx, float errlim,
-             CgState* st, CgState* host_st, float* vec, cudaStream_t s, int* iters_out) {
+// div B projection of one box.  With graphs (the context's cache), the
+// solver's iterations are replayed graphs; without (the no-allocation entry,
+// which must not create any), plain launches.
+int run_divb_with(g3m3_ctx* c, float* bx, float* by, float* bz, const Dims& d, float rx, float errlim,
+                  CgState* st, CgState* host_st, float* vec, cudaStream_t s, int* iters_out, CgGraphs* graphs) {
   DivbArgs a{};
   a.bx = bx; a.by = by; a.bz = bz;
   const size_t n = d.cells();
@@ -219,12 +228,17 @@ int run_divb(g3m3_ctx* c, float* bx, float* by, float* bz, const Dims& d, float 
   a.xi = vec + 5 * n; a.xj = vec + 6 * n;
   a.st = st; a.d = d; a.rx = rx; a.ry = rx; a.rz = rx;
   int status = CG_RUNNING;
-  int rc = run_cg(c, a, errlim, false, 1, host_st, s, iters_out, nullptr, &status);
+  int rc = run_cg(c, a, errlim, false, 1, host_st, s, iters_out, nullptr, &status, graphs);
   if (rc) return rc;
   divb_launch_apply(a, s);
   G3M3_CUDA(c, cudaGetLastError());
   if (status == CG_MAXIT) return set_err(c, G3M3_ERR_NOCONV, "div B solver: too many iterations (%d)", host_st->iters);
   return G3M3_OK;
+}
+
+int run_divb(g3m3_ctx* c, float* bx, float* by, float* bz, const Dims& d, float rx, float errlim,
+             CgState* st, CgState* host_st, float* vec, cudaStream_t s, int* iters_out) {
+  return run_divb_with(c, bx, by, bz, d, rx, errlim, st, host_st, vec, s, iters_out, nullptr);
 }
 
 }  // namespace g3m3
@@ -1071,8 +1085,8 @@ int g3m3_divb_correct(g3m3_ctx* ctx, int nx, int ny, int nz, int n_grids, int bo
   float* dby = r.f(by, n4) + o;
   float* dbz = r.f(bz, n4) + o;
   if (r.st) return r.st;
-  return run_divb(ctx, dbx, dby, dbz, Dims{nx, ny, nz}, xs[box - 1], divb_errlim, ctx->cg, ctx->host_cg,
-                  ctx->cgvec, ctx->stream, iters);
+  return run_divb_with(ctx, dbx, dby, dbz, Dims{nx, ny, nz}, xs[box - 1], divb_errlim, ctx->cg, ctx->host_cg,
+                       ctx->cgvec, ctx->stream, iters, &ctx->cg_graphs);
 }
 
 int g3m3_flux_counter(g3m3_ctx* ctx, const float* qpx, const float* qpy, const float* qpz, const float* hpx,
@@ -1133,7 +1147,7 @@ int g3m3_sparse_solver(g3m3_ctx* ctx, int nbands, int npts, const int* divb_band
   // the SAVEd restart count starts at redo_lim for a recursive call (:55-60)
   const int redos0 = (recurse ? redo_lim : 0) + 1;
   float r2 = 0.0f;
-  s = run_cg(ctx, a, divb_errlim, true, redos0, ctx->host_cg, ctx->stream, nullptr, &r2, &status);
+  s = run_cg(ctx, a, divb_errlim, true, redos0, ctx->host_cg, ctx->stream, nullptr, &r2, &status, &ctx->cg_graphs);
   if (s) return s;
   if (residual2) *residual2 = r2;
   if (status == CG_MAXIT) return set_err(ctx, G3M3_ERR_NOCONV, "sparse_solver: too many iterations");

@@ -30,6 +30,7 @@ struct g3m3_ctx {
   g3m3::CgState* host_cg = nullptr;   // pinned
   float* cgvec = nullptr;
   size_t cgvec_cells = 0;
+  g3m3::CgGraphs cg_graphs;           // solver iterations as replayed graphs
 };
 
 namespace g3m3 {

@@ -1,6 +1,9 @@
 // divb.cuh -- state and arguments of the div B conjugate-gradient solver.
 #pragma once
 
+#include <map>
+#include <string>
+
 #include "kargs.cuh"
 
 namespace g3m3 {
@@ -27,6 +30,28 @@ struct DivbArgs {
   int pos[16];
 };
 
+// CUDA graphs of solver iterations.  A chunk of n iterations is 7n small
+// kernels whose launches, not their work, bound a solve on a box that fits
+// in L2; replaying captured graphs of 64, 32, ..., 1 iterations (captured on
+// first use for each argument block) issues a chunk in at most a few graph
+// launches.  The kernels and their order are those of
+// divb_launch_iterations, so the results are the same.
+class CgGraphs {
+ public:
+  CgGraphs() = default;
+  CgGraphs(const CgGraphs&) = delete;
+  CgGraphs& operator=(const CgGraphs&) = delete;
+  ~CgGraphs() { clear(); }
+  // queue n iterations on s; falls back to plain launches where a graph
+  // cannot be captured (s already capturing)
+  cudaError_t iterations(const DivbArgs& a, int n, cudaStream_t s);
+  void clear();
+
+ private:
+  cudaGraphExec_t get(const DivbArgs& a, int m, cudaStream_t s);
+  std::map<std::string, cudaGraphExec_t> execs_;
+};
+
 // one CG solve in flight (the host side of cg_begin / cg_step)
 struct CgRun {
   DivbArgs a;
@@ -35,6 +60,7 @@ struct CgRun {
   int chunk = 8;
   bool first = true;
   int status = 0;
+  CgGraphs* graphs = nullptr;   // null: iterations as plain launches
 };
 
 void divb_launch_init(const DivbArgs& a, cudaStream_t s);

@@ -1048,6 +1048,7 @@ int divb_begin(g3m3_model* m) {
     a.rx = a.ry = a.rz = p.xspac[b - 1];
     r.host_st = m->host_cg_box + (b - 1);
     r.s = m->divb_stream[b - 1];
+    r.graphs = &m->ctx->cg_graphs;
     m->divb_rep[b - 1] = 0;
     m->divb_fin[b - 1] = false;
     G3M3_CUDA(m->ctx, cudaStreamWaitEvent(r.s, m->fork_ev, 0));

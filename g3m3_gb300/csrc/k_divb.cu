@@ -349,4 +349,73 @@ void divb_launch_apply(const DivbArgs& a, cudaStream_t s) {
   k_cg_apply<<<cg_blocks(a.d), TPB, 0, s>>>(a);
 }
 
+namespace {
+// the fields of an argument block that the iteration kernels read (not the
+// field arrays bx, by, bz: only the set-up and the correction touch them,
+// and the engine's buffer roles alternate which arrays those are)
+std::string graph_key(const DivbArgs& a, int m) {
+  const void* ptrs[8] = {a.rhs, a.x, a.xs, a.g, a.h, a.xi, a.xj, a.st};
+  std::string k(reinterpret_cast<const char*>(ptrs), sizeof ptrs);
+  const int ints[5] = {a.d.nx, a.d.ny, a.d.nz, a.nbands, m};
+  k.append(reinterpret_cast<const char*>(ints), sizeof ints);
+  const float fl[3] = {a.rx, a.ry, a.rz};
+  k.append(reinterpret_cast<const char*>(fl), sizeof fl);
+  k.append(reinterpret_cast<const char*>(&a.band), sizeof a.band);
+  if (a.band && a.nbands > 0) k.append(reinterpret_cast<const char*>(a.pos), sizeof(int) * (size_t)a.nbands);
+  return k;
+}
+constexpr int kMaxGraphIters = 64;
+constexpr size_t kMaxGraphs = 2048;  // a bound on the cache (16 members x 5 boxes x 7 lengths fit)
+}  // namespace
+
+cudaGraphExec_t CgGraphs::get(const DivbArgs& a, int m, cudaStream_t s) {
+  const std::string key = graph_key(a, m);
+  auto it = execs_.find(key);
+  if (it != execs_.end()) return it->second;
+  if (execs_.size() >= kMaxGraphs) clear();
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  DivbArgs ai = a;
+  ai.bx = ai.by = ai.bz = nullptr;   // never read by the iteration kernels
+  divb_launch_iterations(ai, m, s);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(s, &g);
+  cudaGraphExec_t ex = nullptr;
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&ex, g, 0);
+  if (g) cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  execs_.emplace(key, ex);
+  return ex;
+}
+
+cudaError_t CgGraphs::iterations(const DivbArgs& a, int n, cudaStream_t s) {
+  // an argument block seen for the first time gets all seven lengths, so
+  // later chunk lengths never capture in the middle of a run
+  if (!execs_.count(graph_key(a, kMaxGraphIters)))
+    for (int m = kMaxGraphIters; m >= 1; m >>= 1) get(a, m, s);
+  while (n > 0) {
+    int m = kMaxGraphIters;
+    while (m > n) m >>= 1;
+    cudaGraphExec_t ex = get(a, m, s);
+    if (ex) {
+      const cudaError_t e = cudaGraphLaunch(ex, s);
+      if (e != cudaSuccess) return e;
+    } else {
+      divb_launch_iterations(a, m, s);
+    }
+    n -= m;
+  }
+  return cudaGetLastError();
+}
+
+void CgGraphs::clear() {
+  for (auto& kv : execs_) cudaGraphExecDestroy(kv.second);
+  execs_.clear();
+}
+
 }  // namespace g3m3
