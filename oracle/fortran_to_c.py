@@ -1165,6 +1165,52 @@ class Gen:
             raise TranslateError(f"{u.name}: unclosed blocks {stack}")
         return out
 
+    def unformatted_io(self, st, out, pad):
+        """OPEN(unit, ..., form='unformatted'), CLOSE(unit) and the
+        unformatted sequential WRITE(unit) item, ... of the fluid (restart)
+        files: unit u goes to <ref_unit_dir>/fort.<u>, each WRITE one record
+        between 4-byte length markers, items in order, whole arrays in
+        storage order.  Formatted output is dropped by the caller."""
+        m = re.match(r"^(open|close|write)\s*\(", st)
+        if not m:
+            return False
+        j = matching_paren(st, m.end() - 1)
+        ctl = split_top(st[m.end():j])
+        if m.group(1) == "open":
+            if not any(re.match(r"^form\s*=\s*'unformatted'$", c) for c in ctl):
+                return False
+            unit = next(c for c in ctl if "=" not in c or c.startswith("unit"))
+            unit = unit.split("=", 1)[1] if unit.startswith("unit") else unit
+            out.append(f"{pad}ref_open_unit((int)({self.ex(parse_expr(unit))[0]}));")
+            return True
+        if m.group(1) == "close":
+            out.append(f"{pad}ref_close_unit((int)({self.ex(parse_expr(ctl[0]))[0]}));")
+            return True
+        if len(ctl) != 1 or ctl[0] == "*" or ctl[0].startswith("'") or "=" in ctl[0]:
+            return False                  # list-directed or formatted
+        unit_c = self.ex(parse_expr(ctl[0]))[0]
+        if ctl[0] in self.u.syms and self.u.type_of(ctl[0]) == "char":
+            return False                  # an internal write
+        ptrs, sizes = [], []
+        for item in split_top(st[j + 1:].strip()):
+            e = parse_expr(item)
+            if e[0] != "name":
+                raise TranslateError(f"{self.u.name}: unformatted item {item!r}")
+            c, t = self.name_ref(e[1])
+            sym = self.u.syms.get(e[1])
+            ct = CTYPE[t[:-2]] if t.endswith("[]") else CTYPE[t]
+            if t.endswith("[]"):
+                cb = self.cn(e[1])
+                ext = " * ".join(f"{cb}_ex{d}" for d in range(len(sym.dims)))
+                ptrs.append(f"(const void*){c}")
+                sizes.append(f"(size_t)({ext}) * sizeof({ct})")
+            else:
+                ptrs.append(f"(const void*)&{c}" if not c.startswith("(*") else f"(const void*){c[2:-1]}")
+                sizes.append(f"sizeof({ct})")
+        out.append(f"{pad}{{ const void* p_[] = {{{', '.join(ptrs)}}}; const size_t n_[] = {{{', '.join(sizes)}}}; "
+                   f"ref_write_record((int)({unit_c}), {len(ptrs)}, p_, n_); }}")
+        return True
+
     def simple(self, st, out, ind, u, ln):
         pad = "  " * ind
         if st == "return":
@@ -1182,8 +1228,10 @@ class Gen:
         if st.startswith("stop") or st.startswith("call exit"):
             out.append(f'{pad}ref_stop("{u.name}");')
             return
+        if self.unformatted_io(st, out, pad):
+            return
         if re.match(r"^(write|print|open|close|read|inquire|rewind|backspace|flush)\b", st):
-            out.append(f"{pad}/* output statement dropped */")
+            out.append(f"{pad}/* formatted or inquiry statement dropped */")
             return
         m = re.match(r"^call\s+(\w+)\s*(\((.*)\))?\s*$", st)
         if m:
@@ -1314,6 +1362,27 @@ class Gen:
             "  ref_main_stopped = 1;",
             "  if (ref_jmp_armed) longjmp(ref_jmp, 1);",
             "  exit(3);",
+            "}",
+            "char ref_unit_dir[512] = \".\";",
+            "static FILE* ref_units[100];",
+            "static void ref_open_unit(int u) {",
+            "  if (u < 0 || u >= 100) return;",
+            "  if (ref_units[u]) fclose(ref_units[u]);",
+            "  char path[640];",
+            "  snprintf(path, sizeof path, \"%s/fort.%d\", ref_unit_dir, u);",
+            "  ref_units[u] = fopen(path, \"wb\");",
+            "}",
+            "static void ref_close_unit(int u) {",
+            "  if (u >= 0 && u < 100 && ref_units[u]) { fclose(ref_units[u]); ref_units[u] = 0; }",
+            "}",
+            "static void ref_write_record(int u, int k, const void** p, const size_t* n) {",
+            "  if (u < 0 || u >= 100 || !ref_units[u]) return;",
+            "  size_t len = 0;",
+            "  for (int i = 0; i < k; i++) len += n[i];",
+            "  const int marker = (int)len;   /* 4-byte record length before and after */",
+            "  fwrite(&marker, 4, 1, ref_units[u]);",
+            "  for (int i = 0; i < k; i++) fwrite(p[i], 1, n[i], ref_units[u]);",
+            "  fwrite(&marker, 4, 1, ref_units[u]);",
             "}",
             "static void ref_untranslated(const char* who) {",
             "  ref_untranslated_calls++;",

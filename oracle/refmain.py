@@ -91,6 +91,13 @@ class RefMain:
             a = np.ascontiguousarray(np.asarray(v, dtype=_NP[m["type"]]).ravel())
             ctypes.memmove(base + m["offset"], a.ctypes.data, a.nbytes)
 
+    def set_unit_dir(self, path):
+        """Directory where the loop's unformatted units (the fluid files,
+        unit fluid_f) are written as fort.<unit>."""
+        b = os.fsencode(path)[:511] + b"\0"
+        buf = (ctypes.c_char * 512).in_dll(self.lib, "ref_unit_dir")
+        ctypes.memmove(ctypes.addressof(buf), b, len(b))
+
     # ---- running ----
     def init_steps(self):
         """The reference's time-step set-up before its loop (density and

@@ -147,3 +147,38 @@ print("SAME" if same.all() else "DIFF %d" % (~same).sum())
                        capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr[-2000:]
     assert r.stdout.strip().endswith("SAME"), r.stdout[-500:]
+
+
+def test_fluid_file_matches_reference_writer(tmp_path):
+    """The fluid (restart) file the reference's main loop writes at a
+    fluid-file time (3d_main.f90:3305-3349: unformatted records of t, the 34
+    fields, b0 and the inner-boundary lists) equals, byte for byte, what
+    g3m3_fluid_write makes of the same state."""
+    import ctypes
+    import os
+    from g3m3_gb300 import _lib
+    from g3m3_gb300.api import addr
+    from g3m3_gb300.state import make_config
+    from oracle.oracle import OracleModel
+    probe = OracleModel(make_config("tiny3"))
+    probe.init_steps()
+    probe.main_step()
+    om, rm = _pair("tiny3", divb_at=probe.s.t)
+    rm.set(divb_lores=0)           # the file only: no div B pass after it
+    rm.set_unit_dir(str(tmp_path))
+    rm.steps(1)
+    om.main_step()
+    _compare(om, rm, "tiny3 after the step that writes the file")
+    ref = open(os.path.join(str(tmp_path), "fort.11"), "rb").read()
+    li = {k: np.ascontiguousarray(v) for k, v in om.lists.items()}
+    path = str(tmp_path / "ours")
+    L = _lib.load()
+    rc = L.g3m3_fluid_write(None, path.encode(), ctypes.byref(om.p), ctypes.c_double(om.s.t), addr(om.cur),
+                            addr(om.b0), addr(li["parm_srf"]), addr(li["parm_mid"]), addr(li["parm_zero"]),
+                            addr(li["ijzero"]), addr(li["numzero"]), addr(li["ijmid"]), addr(li["nummid"]),
+                            addr(li["ijsrf"]), addr(li["numsrf"]), li["ijsrf"].shape[0], li["ijmid"].shape[0],
+                            li["ijzero"].shape[0])
+    assert rc == 0
+    ours = open(path, "rb").read()
+    assert len(ours) == len(ref)
+    assert ours == ref
