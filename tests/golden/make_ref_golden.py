@@ -1,7 +1,7 @@
 """Writes tests/golden/ref_digests.json: SHA-256 digests of the reference's
 own results for every per-routine case of tests/_refcases.py, and of its
 main loop on the one-box 61x61x31 grid (20 main steps) and the production
-nested grid (5 boxes of 121x121x61, one main step).
+nested grid (5 boxes of 121x121x61, after 1 and 10 main steps).
 
 The results come from the reference's Fortran routines translated to C and
 compiled by oracle/fortran_to_c.py (oracle/_ref/libg3m3_ref.so), so this
@@ -46,8 +46,8 @@ def digests(results):
 
 # main-loop cases: (name, grid, build with OpenMP, digest after these main
 # steps) -- BASELINE's one-box 61x61x31 grid for 20 steps and the production
-# nested grid (5 boxes of 121x121x61) for one main step, no div B pass
-MAIN_CASES = [("small", "small", False, [1, 5, 20]), ("nested", "nested", True, [1])]
+# nested grid (5 boxes of 121x121x61) for 10 main steps, no div B pass
+MAIN_CASES = [("small", "small", False, [1, 5, 20]), ("nested", "nested", True, [1, 10])]
 
 
 def main_start(name):
