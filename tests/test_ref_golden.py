@@ -61,8 +61,8 @@ def digest_of(a):
 @pytest.mark.parametrize("name", sorted(GOLDEN["main"]))
 def test_oracle_main_loop_reproduces_reference(name):
     """The reference's main loop on the one-box 61x61x31 grid (20 steps) and
-    on the production nested grid (one main step): the oracle's steps give
-    its digests."""
+    on the production nested grid (its first main step): the oracle's steps
+    give its digests."""
     from golden.make_ref_golden import main_start
     from oracle.oracle import OracleModel
     st, old, wrk = main_start(name)
@@ -70,7 +70,10 @@ def test_oracle_main_loop_reproduces_reference(name):
     assert np.array_equal(om.old, old) and np.array_equal(om.wrk, wrk)
     om.init_steps()
     done = 0
-    for n in sorted(int(k) for k in GOLDEN["main"][name]):
+    steps = sorted(int(k) for k in GOLDEN["main"][name])
+    if name == "nested":
+        steps = steps[:1]      # one production main step takes the CPU about 10 s; the GPU test runs all
+    for n in steps:
         while done < n:
             assert om.main_step() == 0
             done += 1
