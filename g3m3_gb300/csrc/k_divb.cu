@@ -218,11 +218,6 @@ __global__ void k_cg_control(DivbArgs a) {
     s->status = CG_CONVERGED;
   } else if (r2 > s->rsq) {
     s->status = CG_RESTART;            // the host restores x and restarts
-  } else if (r2 != r2) {
-    // a NaN residual (an exactly divergence-free B makes the step 0/0) never
-    // passes a test again: the reference iterates to 10*npts with x already
-    // NaN; stop now with the same result and the same not-converged status
-    s->status = CG_MAXIT;
   } else if (s->iters >= s->maxit) {
     s->status = CG_MAXIT;
   } else {
@@ -259,7 +254,14 @@ __global__ void k_cg_control2(DivbArgs a) {
   CgState* s = a.st;
   if (s->status != CG_RUNNING) return;
   if (s->gg == 0.0) {
-    s->status = CG_CONVERGED;
+    s->status = CG_CONVERGED;          // the reference's return at gg = 0 (:142)
+  } else if (s->r2_last != s->r2_last) {
+    // a NaN residual never passes a test again: the reference iterates on
+    // to 10*npts with x already NaN; stop now with the same result and the
+    // same not-converged status.  (An exactly divergence-free B gives NaN
+    // from 0/0 with g = 0, and returns through the test above, as the
+    // reference does after its first iteration.)
+    s->status = CG_MAXIT;
   } else {
     s->gam = (float)(s->dgg / s->gg);
   }

@@ -421,6 +421,27 @@ def c_divb_correct(side, cfg, box, errlim):
     return uniform(side, "divb_correct", args)
 
 
+def c_divb_zero(side):
+    """An exactly divergence-free B (uniform): the first iteration divides
+    0/0, x becomes NaN and the solver returns through its gg = 0 test; the
+    interior of B becomes NaN on every side alike."""
+    I = Inputs("tiny")
+    p = I.p
+    pos = np.array([p.nx * p.ny, p.nx, 1, 0, -1, -p.nx, -p.nx * p.ny], np.int32)
+    xs = np.array(p.xspac[: p.n_grids], np.float32)
+    b = [np.full_like(I.cur[31 + q], v) for q, v in enumerate((0.3, -0.1, 0.2))]
+    args = I.dims(1) + [7, pos, xs, 1e-4] + b
+    if side != "gpu":
+        return uniform(side, "divb_correct", args)
+    # the library returns an error status unless the solve ends the
+    # reference's way (its gg = 0 return), which Context.call would raise
+    a = copy_args(args)
+    iters = ctypes.c_int()
+    _gpu("divb_correct", a, [ctypes.addressof(iters)])
+    assert iters.value == 1, iters.value
+    return {f"arg{i}": x for i, x in enumerate(a) if isinstance(x, np.ndarray)}
+
+
 def c_sparse_solver(side, recurse, redo_lim, x0):
     nx = ny = nz = 9
     n = nx * ny * nz
@@ -532,6 +553,7 @@ for _box in (1, 2):
         _add(c_flanks_synced, box=_box, q=_q)
 for _cfg, _box, _e in (("tiny2", 1, 1e-4), ("tiny2", 2, 1e-6), ("tiny3", 1, 1e-4)):
     _add(c_divb_correct, gpu=False, cfg=_cfg, box=_box, errlim=_e)
+_add(c_divb_zero)
 for _r, _lim, _x0 in ((0, 0, 0.0), (1, 2, 0.3)):
     _add(c_sparse_solver, gpu=False, recurse=_r, redo_lim=_lim, x0=_x0)
 for _seed in (3, 4):

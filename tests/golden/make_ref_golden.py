@@ -8,7 +8,7 @@ compiled by oracle/fortran_to_c.py (oracle/_ref/libg3m3_ref.so), so this
 needs the reference's sources; the digests it writes let the oracle and the
 library be checked against the reference where the sources are absent.
 
-    python tests/golden/make_ref_golden.py
+    python tests/golden/make_ref_golden.py [--keep-main]
 """
 from __future__ import annotations
 
@@ -97,7 +97,10 @@ def make():
            "cases": {}}
     for cid, fn, kw, _ in CASES:
         out["cases"][cid] = digests(run(cid, "ref"))
-    out["main"] = make_main()
+    if "--keep-main" in sys.argv and os.path.exists(OUT):
+        out["main"] = json.load(open(OUT))["main"]   # the main-loop digests take minutes
+    else:
+        out["main"] = make_main()
     with open(OUT, "w") as fh:
         json.dump(out, fh, indent=0, sort_keys=True)
         fh.write("\n")
