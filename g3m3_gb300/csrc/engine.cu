@@ -1887,12 +1887,20 @@ int g3m3_ensemble_run(g3m3_ensemble* e, int nsteps, int use_graph) {
     // every member's step is ordered after earlier work on the ensemble's
     // stream and the ensemble's stream after every member's step, so events
     // recorded there bracket the whole step in both modes
+    // In the one-graph form the members' steps form kGraphChains chains of
+    // members, one after another within a chain, and each member's stages
+    // run on its own stream only (its side streams folded in): the graph
+    // executor overlapped 16 member branches of four streams each far worse
+    // (542 M cell-updates/s on the 16-member bench ensemble) than 2 chains
+    // of single-stream members (765 M; 4 chains 706 M, 8 659 M, 1 649 M).
+    constexpr size_t kGraphChains = 2;
     auto fork_join = [&](bool capture_mode) -> int {
       int64_t nk = 0;
       if ((ce = cudaEventRecord(e->fork, origin)) != cudaSuccess) return cuda_check(e->ctx, ce, "fork");
       for (size_t i = 0; i < nm; i++) {
         g3m3_model* m = e->members[i];
-        if ((ce = cudaStreamWaitEvent(S(m), e->fork, 0)) != cudaSuccess) return cuda_check(e->ctx, ce, "fork");
+        const cudaEvent_t after = (capture_mode && i >= kGraphChains) ? e->done[i - kGraphChains] : e->fork;
+        if ((ce = cudaStreamWaitEvent(S(m), after, 0)) != cudaSuccess) return cuda_check(e->ctx, ce, "fork");
         const int rc = step_enqueue(m, acts[i]);
         if (rc) return rc;
         nk += m->launches_in_step;
@@ -1913,10 +1921,24 @@ int g3m3_ensemble_run(g3m3_ensemble* e, int nsteps, int use_graph) {
         std::vector<Roles> saved(nm);
         for (size_t i = 0; i < nm; i++) saved[i] = save_roles(e->members[i]);
         cudaGraph_t g = nullptr;
-        if ((ce = cudaStreamBeginCapture(origin, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+        // side streams folded into each member's stream for the capture
+        std::vector<std::array<cudaStream_t, 3>> aux_saved(nm);
+        for (size_t i = 0; i < nm; i++) {
+          g3m3_model* mm = e->members[i];
+          for (int q = 0; q < 3; q++) {
+            aux_saved[i][q] = mm->aux[q];
+            mm->aux[q] = S(mm);
+          }
+        }
+        if ((ce = cudaStreamBeginCapture(origin, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
+          for (size_t i = 0; i < nm; i++)
+            for (int q = 0; q < 3; q++) e->members[i]->aux[q] = aux_saved[i][q];
           return cuda_check(e->ctx, ce, "begin capture");
+        }
         const int rc = fork_join(true);
         const cudaError_t e2 = cudaStreamEndCapture(origin, &g);
+        for (size_t i = 0; i < nm; i++)
+          for (int q = 0; q < 3; q++) e->members[i]->aux[q] = aux_saved[i][q];
         for (size_t i = 0; i < nm; i++) restore_roles(e->members[i], saved[i]);
         if (rc || e2 != cudaSuccess) {
           if (g) cudaGraphDestroy(g);
