@@ -452,18 +452,20 @@ def run_reference(args):
 
 
 def run_profile(args):
-    """A single 121x121x61 box (state > L2, < 1 GB on the device) stepped with
-    host-loop launches; used as the small case of the ncu captures."""
+    """One 121x121x61 box (state > L2, < 1 GB on the device), or the first
+    --profile-boxes of the nested grid (2: about 1.5 GB, with flanks and
+    corer), stepped with host-loop launches; the small case of the ncu
+    captures."""
     from g3m3_gb300.api import Context, Model
     from g3m3_gb300.state import make_config
-    st = make_config("nested", n_grids=1, divb_every=0)
+    st = make_config("nested", n_grids=args.profile_boxes, divb_every=0)
     with Context(0) as ctx:
         m = Model(ctx, st)
         variant = m.autotune()   # 24 flux-correction launches, as in the benchmark
         m.init_steps()
         m.run(args.warmup + args.steps, graph=False)
         k, _ = m.stats()
-        print(json.dumps({"profile_case": "1 box 121x121x61", "main_steps": args.warmup + args.steps,
+        print(json.dumps({"profile_case": f"{args.profile_boxes} box(es) 121x121x61", "main_steps": args.warmup + args.steps,
                           "kernel_launches": k, "fcsmooth_variant": variant}))
 
 
@@ -477,6 +479,8 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the 16-member ensemble leg")
     ap.add_argument("--profile", action="store_true",
                     help="profiling case for ncu: one 121x121x61 box, warmup+steps main steps, host-loop launches")
+    ap.add_argument("--profile-boxes", type=int, default=1,
+                    help="nested 121x121x61 boxes of the profiling case (2: flanks and corer run too)")
     args = ap.parse_args()
     if args.profile:
         return run_profile(args)
