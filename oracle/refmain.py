@@ -42,6 +42,11 @@ class RefMain:
             self.meta = json.load(fh)
         self.vars = self.meta["main"]["variables"]
         self.keep = []
+        # fluid files written at fluid-file times go to a scratch directory
+        # unless set_unit_dir chooses one
+        import tempfile
+        self._tmp = tempfile.TemporaryDirectory(prefix="g3m3_ref_units_")
+        self.set_unit_dir(self._tmp.name)
 
     # ---- variables ----
     def _sym(self, name, ctype):
