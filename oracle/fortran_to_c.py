@@ -18,8 +18,10 @@ Semantics, chosen to match how the reference's makefile builds it
 - default REAL is float, REAL(dp)/DOUBLE PRECISION is double, INTEGER and
   LOGICAL are 32-bit; implicit typing i-n integer, a-h/o-z real;
 - every local scalar and fixed-size local array is static and starts at
-  zero (-save -zero); automatic arrays (bounds from dummies) are allocated
-  per call and start at zero;
+  zero (-save -zero); automatic arrays (bounds from dummies), which the
+  reference's build keeps on the stack, get a buffer per call site and
+  recursion depth that is reused, not zeroed, from call to call, except
+  divB_correct's, which start at zero (its solver's first iterate);
 - expressions are evaluated in the declared precision in source order, one
   rounding per operation (compiled with -ffp-contract=off, no fast-math);
   integer powers are multiplications (x**2 = x*x);
@@ -44,6 +46,9 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
+
+# Routines whose automatic arrays start at zero on every call (see unit()).
+ZERO_AUTOMATIC = {"divb_correct"}
 
 # The hot-path routines, one file each (code/<file>.f90).
 FILES = [
@@ -1315,11 +1320,25 @@ class Gen:
                 else:
                     hc = self.ex(hi)[0]
                     lines.append(f"  const long {name}_ex{d} = (long)({hc}) - {name}_lo{d} + 1;")
+        # Automatic arrays (bounds from dummies) live on the stack in the
+        # reference's build: no allocation and no zeroing per call.  Here each
+        # gets a buffer per call site and recursion depth, kept between calls
+        # (sparse_solver calls itself, and the caller's arrays must survive).
+        # Only divB_correct's are zeroed on every call: its soln_vec is the
+        # solver's starting iterate, uninitialised in the reference and zero
+        # here, as everywhere in this build.
+        if setup:
+            lines.append(f"  static int ref_depth_{u.name} = 0;")
+            lines.append(f"  const int d_ = ref_depth_{u.name}++;")
+            lines.append(f"  if (d_ >= 16) ref_stop(\"{u.name}: recursion deeper than 16\");")
+            free.append(f"  ref_depth_{u.name}--;")
         for _, name, ct in setup:
             s = u.syms[name]
             ext = " * ".join(f"{name}_ex{d}" for d in range(len(s.dims)))
-            lines.append(f"  {ct}* {name} = ({ct}*)calloc((size_t)({ext}) > 0 ? (size_t)({ext}) : 1, sizeof({ct}));")
-            free.append(f"  free({name});")
+            zero = 1 if u.name in ZERO_AUTOMATIC else 0
+            lines.append(f"  static void* {name}_buf[16]; static size_t {name}_cap[16];")
+            lines.append(f"  {ct}* {name} = ({ct}*)ref_auto(&{name}_buf[d_], &{name}_cap[d_], "
+                         f"(size_t)({ext}) * sizeof({ct}), {zero});")
         # section-assignment loop counters are declared in their loops
         out = [f"/* ---- {u.src}: subroutine {u.name} ---- */", head + " {"]
         out += decl + lines + body
@@ -1383,6 +1402,12 @@ class Gen:
             "  fwrite(&marker, 4, 1, ref_units[u]);",
             "  for (int i = 0; i < k; i++) fwrite(p[i], 1, n[i], ref_units[u]);",
             "  fwrite(&marker, 4, 1, ref_units[u]);",
+            "}",
+            "static void* ref_auto(void** buf, size_t* cap, size_t bytes, int zero) {",
+            "  if (bytes == 0) bytes = 1;",
+            "  if (*cap < bytes) { free(*buf); *buf = malloc(bytes); *cap = bytes; if (!*buf) ref_stop(\"out of memory\"); }",
+            "  if (zero) memset(*buf, 0, bytes);",
+            "  return *buf;",
             "}",
             "static void ref_untranslated(const char* who) {",
             "  ref_untranslated_calls++;",
