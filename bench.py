@@ -244,6 +244,7 @@ def run_ours(args):
                                               4: "32x8 tiles, two fields per block, FP32x2, cp.async planes, one barrier per plane, 80 registers",
                                               5: "32x8 tiles, two fields per block, FP32x2, cp.async planes, one barrier per plane, registers unbounded",
                                               6: "32x8 tiles, two fields per block, FP32x2, cp.async planes, one barrier per plane, 55 KB rings, 4 blocks/SM",
+                                              7: "32x16 tiles, two fields per block, FP32x2, cp.async planes, one barrier per plane, 92 KB rings, 2 blocks/SM",
                                               }[fcs_variant]}},
         "other_mode": {"value": cu_p / (ms_p / 1e3), "ms_per_step": ms_p / args.steps,
                        "mode": mode_name[not use_graph]},

@@ -203,8 +203,9 @@ class Model:
         """Times the flux-correction variants (0: 32x8 tiles, 1: 32x16,
         2/3: 32x8 with two fields per block in FP32x2, 3/4 blocks per SM,
         4/5/6: the same with asynchronous plane copies and one barrier per
-        plane, 3/3/4 blocks per SM) on this model's box size and keeps the
-        fastest; returns the chosen variant."""
+        plane, 3/3/4 blocks per SM, 7: that form on 32x16 tiles) on this
+        model's box size and keeps the fastest; returns the chosen
+        variant."""
         v = ctypes.c_int(-1)
         self.ctx.check(self.L.g3m3_model_autotune(self.h, ctypes.byref(v)))
         return v.value

@@ -784,6 +784,7 @@ cudaError_t prepare_fcsmooth() {
   cudaError_t e = prepare_pc<8, 3, 6, 4>();
   if (e == cudaSuccess) e = prepare_pc<8, 2, 6, 4>();
   if (e == cudaSuccess) e = prepare_pc<8, 4, 5, 2>();
+  if (e == cudaSuccess) e = prepare_pc<16, 2, 5, 2>();
   return e;
 }
 
@@ -792,7 +793,8 @@ cudaError_t prepare_fcsmooth() {
 // 4 resident blocks per SM; 4 and 5: the two-field form with asynchronous
 // plane copies and one barrier per plane, registers bounded for 3 or 2
 // blocks per SM (shared memory admits 3); 6: the same with 5-slot old/wrk
-// rings and a 2-slot P1 ring (55 KB), 4 blocks per SM
+// rings and a 2-slot P1 ring (55 KB), 4 blocks per SM; 7: variant 6 on
+// 32x16 tiles (fewer halo cells per output, 92 KB, 2 blocks of 512 per SM)
 void launch_fcsmooth_tiled(const FcsArgs& a, cudaStream_t s, int variant) {
   if (variant == 1) launch_ty<16>(a, s);
   else if (variant == 2) launch_pair<8, 3>(a, s);
@@ -800,6 +802,7 @@ void launch_fcsmooth_tiled(const FcsArgs& a, cudaStream_t s, int variant) {
   else if (variant == 4) launch_pc<8, 3, 6, 4>(a, s);
   else if (variant == 5) launch_pc<8, 2, 6, 4>(a, s);
   else if (variant == 6) launch_pc<8, 4, 5, 2>(a, s);
+  else if (variant == 7) launch_pc<16, 2, 5, 2>(a, s);
   else launch_ty<8>(a, s);
 }
 

@@ -472,7 +472,7 @@ int g3m3_model_craft_records(g3m3_model* m, float* out, int* nsteps);
  * g3m3_model_autotune times each variant on scratch copies of box 1 (the
  * state is not changed), keeps the fastest and reports it; cached step
  * graphs are dropped when the choice changes. */
-#define G3M3_FCS_VARIANTS 7
+#define G3M3_FCS_VARIANTS 8
 int g3m3_model_set_variant(g3m3_model* m, int kernel, int variant);
 int g3m3_model_autotune(g3m3_model* m, int* fcs_variant);
 /* Time bookkeeping: t, t_stepnew(1..n_grids), executed cell-updates. */

@@ -95,7 +95,7 @@ def test_ensemble_autotune_per_box_size():
         ens = Ensemble(ctx, states)
         chosen = ens.autotune()
         assert sorted(chosen) == sorted({(s.params.nx, s.params.ny, s.params.nz) for s in states})
-        assert all(v in range(7) for v in chosen.values())
+        assert all(v in range(8) for v in chosen.values())
         ens.init_steps()
         ens.run(2, graph=True)
         outs = [m.state() for m in ens.members]
