@@ -45,7 +45,7 @@ def digests(results):
 
 
 # main-loop cases: (name, grid, build with OpenMP, digest after these main
-# steps) -- BASELINE's one-box 61x61x31 grid for 20 steps and the production
+# steps) -- the one-box 61x61x31 grid for 20 steps and the production
 # nested grid (5 boxes of 121x121x61) for 10 main steps, no div B pass
 MAIN_CASES = [("small", "small", False, [1, 5, 20]), ("nested", "nested", True, [1, 10])]
 
