@@ -73,13 +73,21 @@ class Clocks:
         self.lines = []
 
     def start(self):
+        """Starts the sampler and returns once its first sample is in (at
+        most 10 s), so that samples cover the timed region from its start;
+        only samples taken after this returns are counted."""
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             threading.Thread(target=self._read, daemon=True).start()
         except Exception:
             self.proc = None
+            return
+        t0 = time.time()
+        while not self.lines and self.proc.poll() is None and time.time() - t0 < 10.0:
+            time.sleep(0.01)
+        self.first = len(self.lines)
 
     def _read(self):
         for line in self.proc.stdout:
@@ -92,6 +100,7 @@ class Clocks:
                 self.proc.wait(timeout=5)
             except Exception:
                 self.proc.kill()
+        self.lines = self.lines[getattr(self, "first", 0):]
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
