@@ -367,7 +367,7 @@ def kernel_table(m, reps=20):
 # on a 121x121x61 box (profiles/*_121x121x61.md)
 NCU_TRAFFIC = {
     "fcsmooth x34": 243.07e6 + 95.59e6,
-    "push_ion": 73.73e6 + 6.58e6,
+    "push_ion": 73.58e6 + 6.19e6,
     "set_rho+set_speed_agrd": 100.11e6 + 4.78e6,
     "flanks x34": 82.79e6 + 4.61e6,
 }
