@@ -364,10 +364,12 @@ def kernel_table(m, reps=20):
 
 
 # DRAM bytes (read + write) per launch from one ncu capture of each kernel
-# on a 121x121x61 box (profiles/*_121x121x61.md)
+# on a 121x121x61 box (profiles/*_121x121x61.md); push_ion's is the mean of
+# the 9 corrector-form launches (30 arrays read, the form the kernel timer
+# runs) of the two-box capture (profiles/hbm_per_kernel_2x121x121x61.md)
 NCU_TRAFFIC = {
     "fcsmooth x34": 243.07e6 + 95.59e6,
-    "push_ion": 73.58e6 + 6.19e6,
+    "push_ion": 113.55e6 + 10.35e6,
     "set_rho+set_speed_agrd": 100.11e6 + 4.78e6,
     "flanks x34": 82.79e6 + 4.61e6,
 }
