@@ -123,7 +123,7 @@ void launch_flux_counter(const FluxArgs& a, cudaStream_t s) { k_flux_counter<<<1
 void launch_velocity_floor(const float* rho, const float* const p[3], float* const v[3], float floor_, size_t n,
                            cudaStream_t s) {
   unsigned b = (unsigned)((n + 255) / 256);
-  if (b > 152 * 8) b = 152 * 8;
+  if (b > 8u * sm_count()) b = 8u * sm_count();
   k_velocity_floor<<<b, 256, 0, s>>>(rho, p[0], p[1], p[2], v[0], v[1], v[2], floor_, n);
 }
 

@@ -305,7 +305,7 @@ __global__ void __launch_bounds__(TPB) k_cg_apply(DivbArgs a) {
 unsigned cg_blocks(const Dims& d) {
   const size_t n = d.cells();
   size_t b = (n + TPB - 1) / TPB;
-  if (b > 152 * 4) b = 152 * 4;   // 4 blocks per SM: fewer FP64 atomics per dot product (timed against 2 and 8)
+  if (b > 4 * (size_t)sm_count()) b = 4 * (size_t)sm_count();   // 4 blocks per SM: fewer FP64 atomics per dot product (timed against 2 and 8)
   return (unsigned)b;
 }
 

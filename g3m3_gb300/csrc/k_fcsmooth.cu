@@ -20,6 +20,7 @@
 // fluxes).
 #include <type_traits>
 
+#include "device.cuh"
 #include "kargs.cuh"
 #include "launch.cuh"
 
@@ -763,10 +764,7 @@ static void launch_pair(const FcsArgs& a, cudaStream_t s) {
 
 template <int TY, int MINB, int NS_, int NPS_>
 static cudaError_t prepare_pc() {
-  static cudaError_t done = cudaFuncSetAttribute(k_fcsmooth_pc<TY, MINB, NS_, NPS_>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)PcLayout<TY, NS_, NPS_>::BYTES);
-  return done;
+  return prepare_smem((const void*)k_fcsmooth_pc<TY, MINB, NS_, NPS_>, (int)PcLayout<TY, NS_, NPS_>::BYTES);
 }
 
 template <int TY, int MINB, int NS_, int NPS_>
@@ -778,8 +776,9 @@ static void launch_pc(const FcsArgs& a, cudaStream_t s) {
   k_fcsmooth_pc<TY, MINB, NS_, NPS_><<<grd, blk, PcLayout<TY, NS_, NPS_>::BYTES, s>>>(a);
 }
 
-// Dynamic shared-memory limits of the forms that need them, set before any
-// capture (the engine calls this when a variant is chosen).
+// Dynamic shared-memory limits of the forms that need them on the current
+// device (contexts call this at creation, the engine when a variant is
+// chosen).
 cudaError_t prepare_fcsmooth() {
   cudaError_t e = prepare_pc<8, 3, 6, 4>();
   if (e == cudaSuccess) e = prepare_pc<8, 2, 6, 4>();

@@ -232,11 +232,12 @@ void launch_guards(const GuardArgs& a, cudaStream_t s) {
 }
 
 void launch_guard_scatter(const ScatterArgs& a, cudaStream_t s) {
-  k_guard_scatter<<<152, 256, 0, s>>>(a);
+  k_guard_scatter<<<sm_count(), 256, 0, s>>>(a);
 }
 
 void launch_copy(float* dst, const float* src, size_t n, cudaStream_t s) {
-  k_copy<<<blocks_for(n, 256) < 152 * 8 ? blocks_for(n, 256) : 152 * 8, 256, 0, s>>>(dst, src, n);
+  const unsigned cap = 8u * sm_count();
+  k_copy<<<blocks_for(n, 256) < cap ? blocks_for(n, 256) : cap, 256, 0, s>>>(dst, src, n);
 }
 
 }  // namespace g3m3

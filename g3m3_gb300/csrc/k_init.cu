@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(256) k_init(const __grid_constant__ InitArgs a
 void launch_init(const InitArgs& a, cudaStream_t s) {
   const size_t n = a.d.cells();
   unsigned blocks = (unsigned)((n + 255) / 256);
-  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (blocks > 16u * sm_count()) blocks = 16u * sm_count();
   k_init<<<blocks, 256, 0, s>>>(a);
 }
 

@@ -10,6 +10,7 @@
 // the centre-only inputs (old state, btot, efld, tv) straight from HBM, so
 // each input is read from HBM about once.  The arithmetic is the per-cell
 // kernel's (k_push.cu), operation for operation.
+#include "device.cuh"
 #include "kargs.cuh"
 #include "launch.cuh"
 
@@ -258,33 +259,30 @@ __global__ void __launch_bounds__(TX* TY, 3) k_push_ion_tiled(const __grid_const
   }
 }
 
-template <bool POW2>
-void set_smem() {
-  static bool done = false;
-  if (!done) {
-    cudaFuncSetAttribute(k_push_ion_tiled<POW2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
-    done = true;
-  }
-}
-
 }  // namespace
+
+cudaError_t prepare_push_ion() {
+  cudaError_t e = prepare_smem((const void*)k_push_ion_tiled<true>, (int)SMEM);
+  if (e == cudaSuccess) e = prepare_smem((const void*)k_push_ion_tiled<false>, (int)SMEM);
+  return e;
+}
 
 void launch_push_ion_tiled(const PushIonArgs& a, cudaStream_t s) {
   const dim3 blk(TX, TY, 1);
   const int tiles = ((a.d.nx + TX - 1) / TX) * ((a.d.ny + TY - 1) / TY);
   const int interior = a.d.nz - 2;
-  // about one resident wave: 152 SMs x 3 blocks (65 KB of shared memory each)
-  int chunks = (456 + tiles - 1) / tiles;
+  // about one resident wave: every SM x 3 blocks (65 KB of shared memory each)
+  int chunks = (3 * sm_count() + tiles - 1) / tiles;
   if (chunks > interior) chunks = interior;
   if (chunks < 1) chunks = 1;
   const int kchunk = (interior + chunks - 1) / chunks;
   chunks = (interior + kchunk - 1) / kchunk;
   const dim3 grd((unsigned)((a.d.nx + TX - 1) / TX), (unsigned)((a.d.ny + TY - 1) / TY), (unsigned)chunks);
+  // if preparing failed, the launch fails and the caller's check reports it
+  prepare_push_ion();
   if (is_pow2(2.0f * a.g.dx) && is_pow2(2.0f * a.g.dy) && is_pow2(2.0f * a.g.dz)) {
-    set_smem<true>();
     k_push_ion_tiled<true><<<grd, blk, SMEM, s>>>(a, kchunk);
   } else {
-    set_smem<false>();
     k_push_ion_tiled<false><<<grd, blk, SMEM, s>>>(a, kchunk);
   }
 }

@@ -2,6 +2,7 @@
 // declarations shared by the C ABI and the step engine.
 #pragma once
 
+#include "device.cuh"
 #include "kargs.cuh"
 
 namespace g3m3 {
