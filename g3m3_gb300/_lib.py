@@ -20,6 +20,7 @@ _C2CT = {
     "float": ctypes.c_float,
     "double": ctypes.c_double,
     "void": None,
+    "size_t": ctypes.c_size_t,
 }
 
 
@@ -28,7 +29,7 @@ def header_functions(path: str = HEADER, prefix: str = "g3m3_"):
     text = open(path).read()
     text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
     out = []
-    for m in re.finditer(r"\b(int|void\s*\*|const\s+char\s*\*|void)\s+(" + prefix + r"\w+)\s*\(([^;{]*?)\)\s*;", text, re.S):
+    for m in re.finditer(r"\b(int|size_t|void\s*\*|const\s+char\s*\*|void)\s+(" + prefix + r"\w+)\s*\(([^;{]*?)\)\s*;", text, re.S):
         ret, name, params = m.group(1), m.group(2), m.group(3)
         plist = [] if params.strip() in ("", "void") else [p.strip() for p in params.split(",")]
         out.append((name, " ".join(ret.split()), plist))
@@ -50,6 +51,8 @@ def ctype_of(param: str):
 def restype_of(ret: str):
     if ret == "int":
         return ctypes.c_int
+    if ret == "size_t":
+        return ctypes.c_size_t
     if ret == "void":
         return None
     if "char" in ret:

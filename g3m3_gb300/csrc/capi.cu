@@ -1,5 +1,6 @@
 // capi.cu -- the drop-in C ABI (include/g3m3.h): context, host-array
 // mirrors and one entry point per reference routine.
+#include <cmath>
 #include <cstdarg>
 #include <cstring>
 
@@ -35,7 +36,22 @@ static bool is_device_ptr(const void* p) {
   return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
 }
 
-void* resolve(g3m3_ctx* c, const void* p, size_t bytes, int* status) {
+cudaError_t dev_alloc(g3m3_ctx* c, void** p, size_t bytes) {
+  *p = nullptr;
+  if (c && c->alloc_limit && c->alloc_used + bytes > c->alloc_limit) return cudaErrorMemoryAllocation;
+  const cudaError_t e = cudaMalloc(p, bytes);
+  if (e == cudaSuccess && c) c->alloc_used += bytes;
+  return e;
+}
+
+bool finite_ok(const g3m3_ctx* c, const float* p, size_t n) {
+  if (!c || !c->check_finite || !p) return true;
+  for (size_t i = 0; i < n; i++)
+    if (!std::isfinite(p[i])) return false;
+  return true;
+}
+
+void* resolve(g3m3_ctx* c, const void* p, size_t bytes, int* status, bool floats) {
   if (*status) return nullptr;
   if (!p) {
     *status = set_err(c, G3M3_ERR_ARG, "null array argument");
@@ -51,8 +67,12 @@ void* resolve(g3m3_ctx* c, const void* p, size_t bytes, int* status) {
     }
     return it->second.dev;
   }
+  if (floats && !finite_ok(c, static_cast<const float*>(p), bytes / sizeof(float))) {
+    *status = set_err(c, G3M3_ERR_NONFINITE, "host array %p holds NaN or Inf", p);
+    return nullptr;
+  }
   void* d = nullptr;
-  cudaError_t e = cudaMalloc(&d, bytes);
+  cudaError_t e = dev_alloc(c, (void**)&d, bytes);
   if (e != cudaSuccess) {
     *status = cuda_check(c, e, "cudaMalloc(mirror)");
     return nullptr;
@@ -63,8 +83,21 @@ void* resolve(g3m3_ctx* c, const void* p, size_t bytes, int* status) {
     *status = cuda_check(c, e, "cudaMemcpyAsync(mirror upload)");
     return nullptr;
   }
-  c->mirrors[p] = {d, bytes};
+  c->mirrors[p] = {d, bytes, floats};
   return d;
+}
+
+// Small host copies of integer parameter arrays (the band layout), read on
+// the context's stream so that they follow the caller's earlier work there.
+int host_ints(g3m3_ctx* c, const int* p, int n, int* out) {
+  if (!p) return set_err(c, G3M3_ERR_ARG, "null integer array");
+  if (is_device_ptr(p)) {
+    G3M3_CUDA(c, cudaMemcpyAsync(out, p, n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    G3M3_CUDA(c, cudaStreamSynchronize(c->stream));
+    return G3M3_OK;
+  }
+  std::memcpy(out, p, n * sizeof(int));
+  return G3M3_OK;
 }
 
 bool host_floats(g3m3_ctx* c, const float* p, int n, float* out) {
@@ -86,21 +119,21 @@ bool host_floats(g3m3_ctx* c, const float* p, int n, float* out) {
 int ensure_guard_scratch(g3m3_ctx* c, size_t cells) {
   const size_t need = 3 * cells;
   if (!c->words) {
-    G3M3_CUDA(c, cudaMalloc(&c->words, 16 * sizeof(unsigned)));
+    G3M3_CUDA(c, dev_alloc(c, (void**)&c->words, 16 * sizeof(unsigned)));
     G3M3_CUDA(c, cudaMallocHost(&c->host_words, 16 * sizeof(unsigned)));
   }
   if (c->guard_cap >= need) return G3M3_OK;
   if (c->guard_list) cudaFree(c->guard_list);
   c->guard_list = nullptr;
   c->guard_cap = 0;
-  G3M3_CUDA(c, cudaMalloc(&c->guard_list, need * 11 * sizeof(float)));
+  G3M3_CUDA(c, dev_alloc(c, (void**)&c->guard_list, need * 11 * sizeof(float)));
   c->guard_cap = need;
   return G3M3_OK;
 }
 
 int ensure_words(g3m3_ctx* c) {
   if (!c->words) {
-    G3M3_CUDA(c, cudaMalloc(&c->words, 16 * sizeof(unsigned)));
+    G3M3_CUDA(c, dev_alloc(c, (void**)&c->words, 16 * sizeof(unsigned)));
     G3M3_CUDA(c, cudaMallocHost(&c->host_words, 16 * sizeof(unsigned)));
   }
   return G3M3_OK;
@@ -108,14 +141,14 @@ int ensure_words(g3m3_ctx* c) {
 
 int ensure_cg_scratch(g3m3_ctx* c, size_t cells) {
   if (!c->cg) {
-    G3M3_CUDA(c, cudaMalloc(&c->cg, sizeof(CgState)));
+    G3M3_CUDA(c, dev_alloc(c, (void**)&c->cg, sizeof(CgState)));
     G3M3_CUDA(c, cudaMallocHost(&c->host_cg, sizeof(CgState)));
   }
   if (c->cgvec_cells >= cells) return G3M3_OK;
   if (c->cgvec) cudaFree(c->cgvec);
   c->cgvec = nullptr;
   c->cgvec_cells = 0;
-  G3M3_CUDA(c, cudaMalloc(&c->cgvec, 7 * cells * sizeof(float)));
+  G3M3_CUDA(c, dev_alloc(c, (void**)&c->cgvec, 7 * cells * sizeof(float)));
   c->cgvec_cells = cells;
   return G3M3_OK;
 }
@@ -145,7 +178,8 @@ int cg_begin(g3m3_ctx* c, CgRun& r, float errlim, bool given, int redos0, int hi
   const float e2 = (float)n * (errlim * errlim);   // sub_sparse_solver.f90:53 in FP32
   init.errlim2 = (double)e2;
   init.status = CG_RUNNING;
-  init.maxit = (int)((10L * (long)n) > 2000000000L ? 2000000000L : 10L * (long)n);
+  init.maxit = (int)((10L * (long)n) > 2000000000L ? 2000000000L : 10L * (long)n);   // :80
+  if (c->cg_maxit > 0 && c->cg_maxit < init.maxit) init.maxit = c->cg_maxit;
   init.redos = redos0;
   *r.host_st = init;
   G3M3_CUDA(c, cudaMemcpyAsync(r.a.st, r.host_st, sizeof(CgState), cudaMemcpyHostToDevice, r.s));
@@ -205,12 +239,16 @@ int run_cg(g3m3_ctx* c, const DivbArgs& a, float errlim, bool given, int redos0,
            cudaStream_t s, int* iters_out, float* residual2_out, int* status_out, CgGraphs* graphs = nullptr) {
   CgRun r;
   r.a = a; r.host_st = host_st; r.s = s; r.graphs = graphs;
-  int rc = cg_begin(c, r, errlim, given, redos0, c->cg_hint);
+  // replayed graphs make a long first chunk cheap to issue; plain launches
+  // (the no-allocation entry) keep their own hint, capped, so that a hint
+  // from a larger box cannot queue thousands of launches before the first poll
+  int& hint = graphs ? c->cg_hint : c->cg_hint_plain;
+  int rc = cg_begin(c, r, errlim, given, redos0, graphs ? hint : (hint < 64 ? hint : 64));
   bool done = false;
   while (rc == G3M3_OK && !done) rc = cg_step(c, r, &done);
   if (rc) return rc;
   if (iters_out) *iters_out = host_st->iters;
-  if (r.status == CG_CONVERGED && host_st->iters > 0 && host_st->iters <= 4096) c->cg_hint = host_st->iters;
+  if (r.status == CG_CONVERGED && host_st->iters > 0 && host_st->iters <= 4096) hint = host_st->iters;
   if (residual2_out) *residual2_out = (float)host_st->r2_last;
   if (status_out) *status_out = r.status;
   return G3M3_OK;
@@ -251,7 +289,7 @@ struct Res {
   g3m3_ctx* c;
   int st = 0;
   explicit Res(g3m3_ctx* cc) : c(cc) {}
-  float* f(const float* p, size_t n) { return static_cast<float*>(resolve(c, p, n * sizeof(float), &st)); }
+  float* f(const float* p, size_t n) { return static_cast<float*>(resolve(c, p, n * sizeof(float), &st, true)); }
   int* i(const int* p, size_t n) { return static_cast<int*>(resolve(c, p, n * sizeof(int), &st)); }
 };
 
@@ -307,6 +345,12 @@ int g3m3_ctx_create(g3m3_ctx** out, int device) {
     return G3M3_ERR_CUDA;
   }
   if (cudaSetDevice(device) != cudaSuccess) return G3M3_ERR_CUDA;
+  // kernels that stage more than 48 KB get their shared-memory limit on
+  // this device now, before any stream capture
+  if (prepare_device_kernels() != cudaSuccess) {
+    cudaGetLastError();
+    return G3M3_ERR_CUDA;
+  }
   g3m3_ctx* c = new g3m3_ctx();
   c->device = device;
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -335,6 +379,26 @@ int g3m3_ctx_destroy(g3m3_ctx* c) {
 
 const char* g3m3_last_error(g3m3_ctx* c) { return c ? c->err.c_str() : "no context"; }
 
+int g3m3_ctx_set_cg_maxit(g3m3_ctx* c, int maxit) {
+  if (!c || maxit < 0) return G3M3_ERR_ARG;
+  c->cg_maxit = maxit;
+  return G3M3_OK;
+}
+
+int g3m3_ctx_set_finite_check(g3m3_ctx* c, int on) {
+  if (!c) return G3M3_ERR_ARG;
+  c->check_finite = on != 0;
+  return G3M3_OK;
+}
+
+int g3m3_ctx_set_alloc_limit(g3m3_ctx* c, size_t bytes) {
+  if (!c) return G3M3_ERR_ARG;
+  c->alloc_limit = bytes;
+  return G3M3_OK;
+}
+
+size_t g3m3_ctx_allocated(g3m3_ctx* c) { return c ? c->alloc_used : 0; }
+
 int g3m3_synchronize(g3m3_ctx* c) {
   if (!c) return G3M3_ERR_ARG;
   G3M3_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -354,6 +418,8 @@ int g3m3_sync_to_device(g3m3_ctx* c, const void* p) {
   if (!c || !p) return G3M3_ERR_ARG;
   auto it = c->mirrors.find(p);
   if (it == c->mirrors.end()) return G3M3_OK;
+  if (it->second.floats && !finite_ok(c, static_cast<const float*>(p), it->second.bytes / sizeof(float)))
+    return set_err(c, G3M3_ERR_NONFINITE, "host array %p holds NaN or Inf", p);
   G3M3_CUDA(c, cudaMemcpyAsync(it->second.dev, p, it->second.bytes, cudaMemcpyHostToDevice, c->stream));
   G3M3_CUDA(c, cudaStreamSynchronize(c->stream));
   return G3M3_OK;
@@ -1069,8 +1135,7 @@ int g3m3_divb_correct(g3m3_ctx* ctx, int nx, int ny, int nz, int n_grids, int bo
   if (nbands != 7) return set_err(ctx, G3M3_ERR_ARG, "divB_correct supports the 7-band Laplacian only");
   if (divb_band_pos) {
     int pos[7];
-    if (is_device_ptr(divb_band_pos)) G3M3_CUDA(ctx, cudaMemcpy(pos, divb_band_pos, sizeof pos, cudaMemcpyDeviceToHost));
-    else std::memcpy(pos, divb_band_pos, sizeof pos);
+    if ((s = host_ints(ctx, divb_band_pos, 7, pos))) return s;
     const int want[7] = {nx * ny, nx, 1, 0, -1, -nx, -nx * ny};
     for (int q = 0; q < 7; q++)
       if (pos[q] != want[q]) return set_err(ctx, G3M3_ERR_ARG, "unexpected band layout");
@@ -1127,10 +1192,9 @@ int g3m3_sparse_solver(g3m3_ctx* ctx, int nbands, int npts, const int* divb_band
   if (nbands < 1 || nbands > 16 || npts < 1 || !divb_band_pos)
     return set_err(ctx, G3M3_ERR_ARG, "sparse_solver: nbands=%d (1..16), npts=%d", nbands, npts);
   DivbArgs a{};
-  if (is_device_ptr(divb_band_pos))
-    G3M3_CUDA(ctx, cudaMemcpy(a.pos, divb_band_pos, nbands * sizeof(int), cudaMemcpyDeviceToHost));
-  else std::memcpy(a.pos, divb_band_pos, nbands * sizeof(int));
-  int s = ensure_cg_scratch(ctx, (size_t)npts);
+  int s = host_ints(ctx, divb_band_pos, nbands, a.pos);
+  if (s) return s;
+  s = ensure_cg_scratch(ctx, (size_t)npts);
   if (s) return s;
   Res r(ctx);
   const size_t n = (size_t)npts;

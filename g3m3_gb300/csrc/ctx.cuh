@@ -16,14 +16,20 @@ struct g3m3_ctx {
   struct Mirror {
     void* dev;
     size_t bytes;
+    bool floats;                      // FP32 data (checked for NaN/Inf when checks are on)
   };
   std::unordered_map<const void*, Mirror> mirrors;
   std::string err;
   float iso_flag = 1.0f;   // set_speed_agrd's SAVEd iso_flag
+  bool check_finite = false;          // reject host-staged FP32 inputs holding NaN or Inf
+  size_t alloc_limit = 0;             // device bytes this context may allocate (0: no limit)
+  size_t alloc_used = 0;              // device bytes allocated so far (never decremented)
   // scratch for the drop-in routines, grown on demand
   float* guard_list = nullptr;
   size_t guard_cap = 0;    // entries
-  int cg_hint = 0;                    // iterations of the last converged CG solve
+  int cg_hint = 0;                    // iterations of the last converged CG solve (graph-replayed)
+  int cg_hint_plain = 0;              // the same for solves issued as plain launches
+  int cg_maxit = 0;                   // iteration cap of every solve (0: the reference's 10 npts)
   unsigned* words = nullptr;          // [0] list count, [1..5] maxima
   unsigned* host_words = nullptr;     // pinned
   g3m3::CgState* cg = nullptr;
@@ -40,11 +46,19 @@ int cuda_check(g3m3_ctx* c, cudaError_t e, const char* what);
 
 // Device address for an array argument of `bytes` bytes: device and managed
 // pointers pass through; a host array gets (or reuses) its mirror.
-void* resolve(g3m3_ctx* c, const void* p, size_t bytes, int* status);
+void* resolve(g3m3_ctx* c, const void* p, size_t bytes, int* status, bool floats = false);
+
+// cudaMalloc charged to the context's allocation budget (g3m3_ctx_set_alloc_limit):
+// over the budget it fails as cudaMalloc does when the device is full.
+cudaError_t dev_alloc(g3m3_ctx* c, void** p, size_t bytes);
+
+// Host FP32 data free of NaN and Inf (always true while checks are off).
+bool finite_ok(const g3m3_ctx* c, const float* p, size_t n);
 
 // Small host copies of parameter arrays (grd_*, xspac) that may live on
 // either side.
 bool host_floats(g3m3_ctx* c, const float* p, int n, float* out);
+int host_ints(g3m3_ctx* c, const int* p, int n, int* out);
 
 int ensure_guard_scratch(g3m3_ctx* c, size_t cells);
 int ensure_cg_scratch(g3m3_ctx* c, size_t cells);

@@ -21,6 +21,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "ctx.cuh"
 
 namespace g3m3 {
@@ -38,6 +40,23 @@ void launch_bande_interior(const BandEArgs& a, cudaStream_t s);
 }  // namespace g3m3
 
 using namespace g3m3;
+
+namespace {
+
+// NVTX ranges around the stages of a box-step, the main step and the div B
+// pass, so that a profiler can attribute host-launched kernels to them (in
+// a replayed graph the kernels carry the range of the replay).
+struct Range {
+  explicit Range(const char* name) { nvtxRangePushA(name); }
+  ~Range() { nvtxRangePop(); }
+  Range(const Range&) = delete;
+  Range& operator=(const Range&) = delete;
+};
+
+const char* const kBoxStepRange[8] = {"box-step 1", "box-step 2", "box-step 3", "box-step 4",
+                                      "box-step 5", "box-step 6", "box-step 7", "box-step 8+"};
+
+}  // namespace
 
 struct g3m3_model {
   g3m3_ctx* ctx = nullptr;
@@ -491,68 +510,78 @@ void apply_role_swaps(g3m3_model* m, const std::vector<Action>& acts) {
 int enqueue_box_step(g3m3_model* m, const Action& act) {
   const g3m3_params& p = m->p;
   const int ng = p.n_grids, b = act.box;
+  Range box_range(kBoxStepRange[b - 1 < 8 ? b - 1 : 7]);
   std::swap(m->role_cur[b - 1], m->role_old[b - 1]);   // store_array
   int st;
-  // predictor (reads of cur are served from old, which holds the same data)
-  fields_stage(m, O, b);
-  push_stage(m, W, O, b, act.s_half, false);
-  boundary_stage(m, W, b, act.s_t1p);
-  if ((st = guard_stage(m, W, b, true, false))) return st;
-  // corrector
-  fields_stage(m, W, b);
-  push_stage(m, C, W, b, act.s_full, true);
-  if (b == ng) {
-    boundary_stage(m, C, b, -1);
-  } else {
-    // the reference applies the corrector's flanks to the wrk arrays
-    // (3d_main.f90:2599-2637) and bndry_inner to cur (:2640-2658).  The
-    // coarse box stays fixed through this box-step, so the interpolated
-    // flank values at the corrector's time are kept for the two later
-    // stages, which use the same time weight.
-    boundary_stage(m, W, b, act.s_t1c, C, FLANKS_KEEP);
+  {
+    // predictor (reads of cur are served from old, which holds the same data)
+    Range r("predictor");
+    fields_stage(m, O, b);
+    push_stage(m, W, O, b, act.s_half, false);
+    boundary_stage(m, W, b, act.s_t1p);
+    if ((st = guard_stage(m, W, b, true, false))) return st;
   }
-  if ((st = guard_stage(m, C, b, true, false))) return st;
-  // Lapidus smoothing (3d_main.f90:2690-2772): the three species beside
-  // the electron-pressure and B chain, each writing its own wrk arrays
-  fork_aux(m);
-  for (int s = 0; s < 3; s++) {
-    LapArgs la{};
-    for (int f = 0; f < 10; f++) {
-      la.in[f] = C(m, 10 * s + f, b);
-      la.out[f] = W(m, 10 * s + f, b);
-      la.chi[f] = f == 0 ? p.chirho : p.chipxyz;
+  {
+    Range r("corrector");
+    fields_stage(m, W, b);
+    push_stage(m, C, W, b, act.s_full, true);
+    if (b == ng) {
+      boundary_stage(m, C, b, -1);
+    } else {
+      // the reference applies the corrector's flanks to the wrk arrays
+      // (3d_main.f90:2599-2637) and bndry_inner to cur (:2640-2658).  The
+      // coarse box stays fixed through this box-step, so the interpolated
+      // flank values at the corrector's time are kept for the two later
+      // stages, which use the same time weight.
+      boundary_stage(m, W, b, act.s_t1c, C, FLANKS_KEEP);
     }
-    la.nf = 10;
-    for (int q = 0; q < 3; q++) la.vp[q] = C(m, 10 * s + 1 + q, b);
-    la.vrho = C(m, 10 * s, b);
-    la.vfloor = p.smallbit;
-    la.d = m->d;
-    la.delt = sref(m, act.s_full);
-    launch_lap(la, m->aux[s]);
+    if ((st = guard_stage(m, C, b, true, false))) return st;
   }
-  VtotArgs va{};
-  for (int s = 0; s < 3; s++) {
-    for (int q = 0; q < 3; q++) va.p[s][q] = C(m, 10 * s + 1 + q, b);
-    va.rho[s] = C(m, 10 * s, b);
+  {
+    // Lapidus smoothing (3d_main.f90:2690-2772): the three species beside
+    // the electron-pressure and B chain, each writing its own wrk arrays
+    Range r("lapidus");
+    fork_aux(m);
+    for (int s = 0; s < 3; s++) {
+      LapArgs la{};
+      for (int f = 0; f < 10; f++) {
+        la.in[f] = C(m, 10 * s + f, b);
+        la.out[f] = W(m, 10 * s + f, b);
+        la.chi[f] = f == 0 ? p.chirho : p.chipxyz;
+      }
+      la.nf = 10;
+      for (int q = 0; q < 3; q++) la.vp[q] = C(m, 10 * s + 1 + q, b);
+      la.vrho = C(m, 10 * s, b);
+      la.vfloor = p.smallbit;
+      la.d = m->d;
+      la.delt = sref(m, act.s_full);
+      launch_lap(la, m->aux[s]);
+    }
+    VtotArgs va{};
+    for (int s = 0; s < 3; s++) {
+      for (int q = 0; q < 3; q++) va.p[s][q] = C(m, 10 * s + 1 + q, b);
+      va.rho[s] = C(m, 10 * s, b);
+    }
+    for (int q = 0; q < 3; q++) va.v[q] = m->vt[q];
+    va.d = m->d;
+    launch_vtot(va, S(m));
+    LapArgs lb{};
+    lb.in[0] = C(m, G3M3_F_EPRES, b); lb.out[0] = W(m, G3M3_F_EPRES, b); lb.chi[0] = p.chipxyz;
+    for (int q = 0; q < 3; q++) {
+      lb.in[1 + q] = C(m, G3M3_F_BX + q, b);
+      lb.out[1 + q] = W(m, G3M3_F_BX + q, b);
+      lb.chi[1 + q] = p.chierg;
+      lb.v[q] = m->vt[q];
+    }
+    lb.nf = 4; lb.d = m->d; lb.delt = sref(m, act.s_full);
+    launch_lap(lb, S(m));
+    join_aux(m);
+    m->launches_in_step += 5;
+    boundary_stage(m, W, b, act.s_t1c, nullptr, FLANKS_REUSE);
+    if ((st = guard_stage(m, W, b, true, false))) return st;
   }
-  for (int q = 0; q < 3; q++) va.v[q] = m->vt[q];
-  va.d = m->d;
-  launch_vtot(va, S(m));
-  LapArgs lb{};
-  lb.in[0] = C(m, G3M3_F_EPRES, b); lb.out[0] = W(m, G3M3_F_EPRES, b); lb.chi[0] = p.chipxyz;
-  for (int q = 0; q < 3; q++) {
-    lb.in[1 + q] = C(m, G3M3_F_BX + q, b);
-    lb.out[1 + q] = W(m, G3M3_F_BX + q, b);
-    lb.chi[1 + q] = p.chierg;
-    lb.v[q] = m->vt[q];
-  }
-  lb.nf = 4; lb.d = m->d; lb.delt = sref(m, act.s_full);
-  launch_lap(lb, S(m));
-  join_aux(m);
-  m->launches_in_step += 5;
-  boundary_stage(m, W, b, act.s_t1c, nullptr, FLANKS_REUSE);
-  if ((st = guard_stage(m, W, b, true, false))) return st;
   // flux correction (3d_main.f90:2896-3036)
+  Range r("flux_correct");
   FcsArgs fa{};
   for (int q = 0; q < G3M3_NFIELDS; q++) {
     fa.px[q] = C(m, q, b);
@@ -613,7 +642,7 @@ int alloc_model(g3m3_model* m) {
   const size_t n3 = m->n3, n4 = m->n4;
   const int mb = m->p.mbndry;
   size_t total = 3 * G3M3_NFIELDS * n4 + 3 * n4 + 2 * (size_t)mb * n3 + 19 * n3 + 7 * n3;
-  cudaError_t e = cudaMalloc(&m->mem, total * sizeof(float));
+  cudaError_t e = dev_alloc(m->ctx, (void**)&m->mem, total * sizeof(float));
   if (e != cudaSuccess) return cuda_check(m->ctx, e, "cudaMalloc(model)");
   e = cudaMemsetAsync(m->mem, 0, total * sizeof(float), S(m));
   if (e != cudaSuccess) return cuda_check(m->ctx, e, "memset(model)");
@@ -630,20 +659,20 @@ int alloc_model(g3m3_model* m) {
   for (int i = 0; i < 19; i++) { *scr[i] = q; q += n3; }
   m->cgvec = q; q += 7 * n3;
   m->gcap = 3 * n3;
-  e = cudaMalloc(&m->glist, m->gcap * 11 * sizeof(float));
+  e = dev_alloc(m->ctx, (void**)&m->glist, m->gcap * 11 * sizeof(float));
   if (e != cudaSuccess) return cuda_check(m->ctx, e, "cudaMalloc(limiter list)");
-  e = cudaMalloc(&m->flank_ibuf, (size_t)G3M3_NFIELDS * shell_count(m->d, 2) * sizeof(float));
+  e = dev_alloc(m->ctx, (void**)&m->flank_ibuf, (size_t)G3M3_NFIELDS * shell_count(m->d, 2) * sizeof(float));
   if (e != cudaSuccess) return cuda_check(m->ctx, e, "cudaMalloc(flank values)");
   const size_t nwords = 8 + 5 * (size_t)G3M3_MAX_GRIDS;
-  if ((e = cudaMalloc(&m->words, nwords * sizeof(unsigned))) != cudaSuccess) return cuda_check(m->ctx, e, "words");
+  if ((e = dev_alloc(m->ctx, (void**)&m->words, nwords * sizeof(unsigned))) != cudaSuccess) return cuda_check(m->ctx, e, "words");
   if ((e = cudaMemsetAsync(m->words, 0, nwords * sizeof(unsigned), S(m))) != cudaSuccess)
     return cuda_check(m->ctx, e, "words");
   if ((e = cudaMallocHost(&m->host_words, nwords * sizeof(unsigned))) != cudaSuccess)
     return cuda_check(m->ctx, e, "host words");
-  if ((e = cudaMalloc(&m->cg, sizeof(CgState))) != cudaSuccess) return cuda_check(m->ctx, e, "cg");
+  if ((e = dev_alloc(m->ctx, (void**)&m->cg, sizeof(CgState))) != cudaSuccess) return cuda_check(m->ctx, e, "cg");
   if ((e = cudaMallocHost(&m->host_cg, sizeof(CgState))) != cudaSuccess) return cuda_check(m->ctx, e, "cg");
   m->scal_cap = 4096;
-  if ((e = cudaMalloc(&m->d_scal, m->scal_cap * sizeof(float))) != cudaSuccess) return cuda_check(m->ctx, e, "scal");
+  if ((e = dev_alloc(m->ctx, (void**)&m->d_scal, m->scal_cap * sizeof(float))) != cudaSuccess) return cuda_check(m->ctx, e, "scal");
   if ((e = cudaMallocHost(&m->h_scal, m->scal_cap * sizeof(float))) != cudaSuccess)
     return cuda_check(m->ctx, e, "scal");
   for (int b = 0; b < G3M3_MAX_GRIDS; b++) { m->role_cur[b] = 0; m->role_old[b] = 1; }
@@ -855,6 +884,8 @@ void* g3m3_model_stream(g3m3_model* m) { return m ? (void*)S(m) : nullptr; }
 
 int g3m3_model_set_field(g3m3_model* m, int which, int field, const float* data) {
   if (!m || !data || field < 0 || field >= G3M3_NFIELDS || which < 0 || which > 2) return G3M3_ERR_ARG;
+  if (!finite_ok(m->ctx, data, m->n4))
+    return set_err(m->ctx, G3M3_ERR_NONFINITE, "field %d holds NaN or Inf", field);
   // `which` names the logical copy; every box shares the same role mapping
   // only before the first step, so per-box roles are honoured here
   for (int b = 1; b <= m->p.n_grids; b++) {
@@ -930,9 +961,9 @@ int g3m3_model_set_inner(g3m3_model* m, const float* resistive, const int* ijsrf
     if (m->parm[l]) cudaFree(m->parm[l]);
     m->ij[l] = nullptr;
     m->parm[l] = nullptr;
-    if ((e = cudaMalloc(&m->ij[l], (size_t)mb * 3 * ml[l] * sizeof(int))) != cudaSuccess)
+    if ((e = dev_alloc(m->ctx, (void**)&m->ij[l], (size_t)mb * 3 * ml[l] * sizeof(int))) != cudaSuccess)
       return cuda_check(m->ctx, e, "lists");
-    if ((e = cudaMalloc(&m->parm[l], (size_t)mb * 7 * ml[l] * sizeof(float))) != cudaSuccess)
+    if ((e = dev_alloc(m->ctx, (void**)&m->parm[l], (size_t)mb * 7 * ml[l] * sizeof(float))) != cudaSuccess)
       return cuda_check(m->ctx, e, "parms");
     if ((e = cudaMemcpy(m->ij[l], ij[l], (size_t)mb * 3 * ml[l] * sizeof(int), cudaMemcpyDefault)) != cudaSuccess)
       return cuda_check(m->ctx, e, "lists");
@@ -1006,10 +1037,10 @@ int ensure_divb_boxes(g3m3_model* m) {
   if (m->cg_box) return G3M3_OK;
   const int ng = m->p.n_grids;
   cudaError_t e;
-  if ((e = cudaMalloc(&m->cg_box, ng * sizeof(CgState))) != cudaSuccess) return cuda_check(m->ctx, e, "div B state");
+  if ((e = dev_alloc(m->ctx, (void**)&m->cg_box, ng * sizeof(CgState))) != cudaSuccess) return cuda_check(m->ctx, e, "div B state");
   if ((e = cudaMallocHost(&m->host_cg_box, ng * sizeof(CgState))) != cudaSuccess)
     return cuda_check(m->ctx, e, "div B state");
-  if (ng > 1 && (e = cudaMalloc(&m->cgvec_more, (size_t)(ng - 1) * 7 * m->n3 * sizeof(float))) != cudaSuccess)
+  if (ng > 1 && (e = dev_alloc(m->ctx, (void**)&m->cgvec_more, (size_t)(ng - 1) * 7 * m->n3 * sizeof(float))) != cudaSuccess)
     return cuda_check(m->ctx, e, "div B vectors");
   for (int b = 0; b < ng; b++) {
     if ((e = cudaStreamCreateWithFlags(&m->divb_stream[b], cudaStreamNonBlocking)) != cudaSuccess)
@@ -1118,6 +1149,7 @@ int divb_end(g3m3_model* m) {
 
 int g3m3_model_divb_all(g3m3_model* m) {
   if (!m) return G3M3_ERR_ARG;
+  Range range("div B pass");
   int st = divb_begin(m);
   for (bool done = false; !st && !done;) st = divb_poll(m, &done);
   return st ? st : divb_end(m);
@@ -1159,6 +1191,7 @@ int step_graph(g3m3_model* m, const std::vector<Action>& acts, const std::string
 }
 
 int one_step(g3m3_model* m, int use_graph, std::vector<Action>& acts) {
+  Range range("main step");
   cudaStream_t s = S(m);
   std::string key;
   int rc = step_plan(m, acts, key);
@@ -1216,6 +1249,8 @@ int g3m3_model_run(g3m3_model* m, int nsteps, int use_graph) {
 
 int g3m3_model_step_host(g3m3_model* m, const float* in, float* out, int use_graph) {
   if (!m || !in || !out) return G3M3_ERR_ARG;
+  if (!finite_ok(m->ctx, in, (size_t)G3M3_NFIELDS * m->n4))
+    return set_err(m->ctx, G3M3_ERR_NONFINITE, "host state holds NaN or Inf");
   m->kernels = 0;
   m->graph_launches = 0;
   if (!pinned(in)) {   // pageable input: plain upload, then the step
@@ -1403,7 +1438,7 @@ int g3m3_model_graphing(g3m3_model* m, int box, int plane, int index, float* out
   const int na = plane == 0 ? d.ny : d.nz, nb = plane == 2 ? d.ny : d.nx;
   const size_t per = (size_t)na * nb;
   float* dout = nullptr;
-  G3M3_CUDA(m->ctx, cudaMalloc(&dout, 32 * per * sizeof(float)));
+  G3M3_CUDA(m->ctx, dev_alloc(m->ctx, (void**)&dout, 32 * per * sizeof(float)));
   // J, total B, |B|, E of the box as the step computes them (calcur, fnd_evel, BandE)
   fields_stage(m, C, box);
   auto cut = [&](std::initializer_list<const float*> src, int q0) {
@@ -1578,10 +1613,10 @@ int g3m3_model_record_craft(g3m3_model* m, int ncraft, const int* npts, const fl
     m->craft_fields[f] = fields[f];
   }
   const size_t nrec = (size_t)capacity * ncraft * (4 + nf);
-  G3M3_CUDA(m->ctx, cudaMalloc(&m->craft_traj, (size_t)4 * start[ncraft] * sizeof(float)));
-  G3M3_CUDA(m->ctx, cudaMalloc(&m->craft_start, (ncraft + 1) * sizeof(int)));
-  G3M3_CUDA(m->ctx, cudaMalloc(&m->craft_out, nrec * sizeof(float)));
-  G3M3_CUDA(m->ctx, cudaMalloc(&m->craft_count, sizeof(unsigned)));
+  G3M3_CUDA(m->ctx, dev_alloc(m->ctx, (void**)&m->craft_traj, (size_t)4 * start[ncraft] * sizeof(float)));
+  G3M3_CUDA(m->ctx, dev_alloc(m->ctx, (void**)&m->craft_start, (ncraft + 1) * sizeof(int)));
+  G3M3_CUDA(m->ctx, dev_alloc(m->ctx, (void**)&m->craft_out, nrec * sizeof(float)));
+  G3M3_CUDA(m->ctx, dev_alloc(m->ctx, (void**)&m->craft_count, sizeof(unsigned)));
   G3M3_CUDA(m->ctx, cudaMemcpy(m->craft_traj, traj, (size_t)4 * start[ncraft] * sizeof(float), cudaMemcpyDefault));
   G3M3_CUDA(m->ctx, cudaMemcpy(m->craft_start, start.data(), (ncraft + 1) * sizeof(int), cudaMemcpyHostToDevice));
   G3M3_CUDA(m->ctx, cudaMemset(m->craft_count, 0, sizeof(unsigned)));
@@ -1622,8 +1657,8 @@ int g3m3_model_record_fluxes(g3m3_model* m, const float* scale, int capacity) {
   m->kernel_nodes.clear();
   if (capacity == 0) return G3M3_OK;
   const size_t n = (size_t)capacity * m->p.n_grids * 6;
-  G3M3_CUDA(m->ctx, cudaMalloc(&m->flux_hist, n * sizeof(float)));
-  G3M3_CUDA(m->ctx, cudaMalloc(&m->flux_count, sizeof(unsigned)));
+  G3M3_CUDA(m->ctx, dev_alloc(m->ctx, (void**)&m->flux_hist, n * sizeof(float)));
+  G3M3_CUDA(m->ctx, dev_alloc(m->ctx, (void**)&m->flux_count, sizeof(unsigned)));
   G3M3_CUDA(m->ctx, cudaMemsetAsync(m->flux_count, 0, sizeof(unsigned), S(m)));
   G3M3_CUDA(m->ctx, cudaMemsetAsync(m->flux_hist, 0, n * sizeof(float), S(m)));
   std::memcpy(m->flux_scale, scale, m->p.n_grids * sizeof(float));
@@ -1668,7 +1703,7 @@ int g3m3_model_autotune(g3m3_model* m, int* fcs_variant) {
   // scratch copies of box 1's current, old and wrk fields: timing runs on
   // realistic values without touching the state
   float* tmp = nullptr;
-  G3M3_CUDA(m->ctx, cudaMalloc(&tmp, 3 * (size_t)G3M3_NFIELDS * n3 * sizeof(float)));
+  G3M3_CUDA(m->ctx, dev_alloc(m->ctx, (void**)&tmp, 3 * (size_t)G3M3_NFIELDS * n3 * sizeof(float)));
   FcsArgs fa{};
   cudaError_t e = cudaSuccess;
   for (int q = 0; q < G3M3_NFIELDS && e == cudaSuccess; q++) {

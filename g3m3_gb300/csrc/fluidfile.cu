@@ -134,6 +134,8 @@ int g3m3_fluid_write(g3m3_ctx* ctx, const char* path, const g3m3_params* p, doub
                      const int* ijzero, const int* numzero, const int* ijmid, const int* nummid, const int* ijsrf,
                      const int* numsrf, int msrf, int mmid, int mzero) {
   if (!path || !p || !state || !b0) return G3M3_ERR_ARG;
+  if (p->nx < 1 || p->ny < 1 || p->nz < 1 || p->n_grids < 1 || p->mbndry < 0 || p->mbndry > p->n_grids)
+    return fail(ctx, G3M3_ERR_ARG, "bad dimensions for", path);
   const size_t n4 = (size_t)p->nx * p->ny * p->nz * p->n_grids;
   const size_t mb = (size_t)p->mbndry;
   FILE* f = fopen(path, "wb");
@@ -156,6 +158,8 @@ int g3m3_fluid_read(g3m3_ctx* ctx, const char* path, const g3m3_params* p, doubl
                     float* parm_srf, float* parm_mid, float* parm_zero, int* ijzero, int* numzero, int* ijmid,
                     int* nummid, int* ijsrf, int* numsrf, int msrf, int mmid, int mzero) {
   if (!path || !p || !state || !b0 || !t) return G3M3_ERR_ARG;
+  if (p->nx < 1 || p->ny < 1 || p->nz < 1 || p->n_grids < 1 || p->mbndry < 0 || p->mbndry > p->n_grids)
+    return fail(ctx, G3M3_ERR_ARG, "bad dimensions for", path);
   const size_t n4 = (size_t)p->nx * p->ny * p->nz * p->n_grids;
   const size_t mb = (size_t)p->mbndry;
   FILE* f = fopen(path, "rb");
@@ -190,7 +194,7 @@ int g3m3_diff_fields(g3m3_ctx* ctx, int nfields, const float* const* a, const fl
   // pointer tables and the statistics in one scratch block
   const size_t bytes = 2 * nfields * sizeof(float*) + nstat * sizeof(double);
   void* scratch = nullptr;
-  G3M3_CUDA(ctx, cudaMalloc(&scratch, bytes));
+  G3M3_CUDA(ctx, dev_alloc(ctx, (void**)&scratch, bytes));
   const float** tab = static_cast<const float**>(scratch);
   double* dstat = reinterpret_cast<double*>(static_cast<char*>(scratch) + 2 * nfields * sizeof(float*));
   std::vector<const float*> host_tab(2 * nfields);
@@ -200,7 +204,7 @@ int g3m3_diff_fields(g3m3_ctx* ctx, int nfields, const float* const* a, const fl
   if (e == cudaSuccess) e = cudaMemsetAsync(dstat, 0, nstat * sizeof(double), ctx->stream);
   if (e == cudaSuccess) {
     unsigned bx = (unsigned)((n + 255) / 256);
-    if (bx > 152) bx = 152;
+    if (bx > (unsigned)sm_count()) bx = (unsigned)sm_count();
     k_diff<<<dim3(bx, (unsigned)(nfields * n_grids)), 256, 0, ctx->stream>>>(tab, tab + nfields, n, n_grids, dstat);
     e = cudaGetLastError();
   }

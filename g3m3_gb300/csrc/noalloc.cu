@@ -11,13 +11,14 @@
 // device buffers; this variant does neither.
 //
 // The solver's state and its seven vectors live in one file-scope device
-// array, sized for boxes of up to G3M3_NOALLOC_DIVB_MAX_CELLS cells.  The
-// first call on a device looks up the array's address there (with that
-// device current) and keeps it; later calls reuse it.  The array is shared
-// by every call on the device and keeps the last call's contents: each call
-// rewrites the solver state from the host and its first kernel zeroes the
-// iterate; every other vector is written before it is read.  Two calls that
-// overlap in time race on the array.
+// array, sized for boxes of up to G3M3_NOALLOC_DIVB_MAX_CELLS cells.  Every
+// call looks up the array's address on the context's device (with that
+// device current); the lookup allocates nothing, so a device reset between
+// calls leaves no stale address behind.  The array is shared by every call
+// on the device and keeps the last call's contents: each call rewrites the
+// solver state from the host and its first kernel zeroes the iterate; every
+// other vector is written before it is read.  Two calls that overlap in
+// time race on the array.
 #include <cstring>
 #include <mutex>
 
@@ -46,35 +47,33 @@ static __device__ __align__(256) unsigned char divb_noalloc_scratch[kScratchByte
 namespace {
 
 std::mutex setup_mutex;
-void* scratch_address[kMaxDevices];   // per device, found once
 
-// Device address of the scratch array on the context's device; the first
-// call per device makes the lookup with that device current.
+// Device address of the scratch array on the context's device, looked up
+// with that device current.
 int scratch_for(g3m3_ctx* c, void** out) {
   if (c->device < 0 || c->device >= kMaxDevices)
     return set_err(c, G3M3_ERR_ARG, "divb_correct_noalloc: device %d out of range", c->device);
   std::lock_guard<std::mutex> lock(setup_mutex);
-  if (!scratch_address[c->device]) {
-    int prev = -1;
-    G3M3_CUDA(c, cudaGetDevice(&prev));
-    if (prev != c->device) G3M3_CUDA(c, cudaSetDevice(c->device));
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, divb_noalloc_scratch);
-    if (prev != c->device) cudaSetDevice(prev);
-    if (e != cudaSuccess) return cuda_check(c, e, "cudaGetSymbolAddress(div B scratch)");
-    scratch_address[c->device] = p;
-  }
-  *out = scratch_address[c->device];
+  int prev = -1;
+  G3M3_CUDA(c, cudaGetDevice(&prev));
+  if (prev != c->device) G3M3_CUDA(c, cudaSetDevice(c->device));
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, divb_noalloc_scratch);
+  if (prev != c->device) cudaSetDevice(prev);
+  if (e != cudaSuccess) return cuda_check(c, e, "cudaGetSymbolAddress(div B scratch)");
+  *out = p;
   return G3M3_OK;
 }
 
-bool on_device(const void* p) {
+// Device (or managed) memory that the context's device can use directly.
+bool on_device(const g3m3_ctx* c, const void* p) {
   cudaPointerAttributes at;
   if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+  if (at.type == cudaMemoryTypeManaged) return true;
+  return at.type == cudaMemoryTypeDevice && at.device == c->device;
 }
 
 }  // namespace
@@ -95,17 +94,19 @@ extern "C" int g3m3_divb_correct_noalloc(g3m3_ctx* ctx, int nx, int ny, int nz, 
   if (nbands != 7) return set_err(ctx, G3M3_ERR_ARG, "divB_correct supports the 7-band Laplacian only");
   if (divb_band_pos) {
     int pos[7];
-    if (on_device(divb_band_pos)) G3M3_CUDA(ctx, cudaMemcpy(pos, divb_band_pos, sizeof pos, cudaMemcpyDeviceToHost));
-    else std::memcpy(pos, divb_band_pos, sizeof pos);
+    const int rc = host_ints(ctx, divb_band_pos, 7, pos);   // ordered on the context's stream
+    if (rc) return rc;
     const int want[7] = {nx * ny, nx, 1, 0, -1, -nx, -nx * ny};
     for (int q = 0; q < 7; q++)
       if (pos[q] != want[q]) return set_err(ctx, G3M3_ERR_ARG, "unexpected band layout");
   }
   float xs[G3M3_MAX_GRIDS];
   if (!host_floats(ctx, xspac, n_grids, xs)) return set_err(ctx, G3M3_ERR_ARG, "xspac unreadable");
-  if (!bx || !by || !bz || !on_device(bx) || !on_device(by) || !on_device(bz))
+  if (!bx || !by || !bz || !on_device(ctx, bx) || !on_device(ctx, by) || !on_device(ctx, bz))
     return set_err(ctx, G3M3_ERR_ARG,
-                   "divb_correct_noalloc: bx, by, bz must be device memory (a host array would need a device copy)");
+                   "divb_correct_noalloc: bx, by, bz must be device memory of the context's device %d (a host "
+                   "array would need a device copy)",
+                   ctx->device);
   void* scratch = nullptr;
   int s = scratch_for(ctx, &scratch);
   if (s) return s;

@@ -70,6 +70,25 @@ const char* g3m3_version(void);
 /* The context's CUDA stream (cudaStream_t), for event timing by callers. */
 void* g3m3_ctx_stream(g3m3_ctx* ctx);
 
+/* Failure handling.  The reference stops or warns where these report a
+ * status (3d_main.f90:1970-1974; sub_sparse_solver.f90:93,157).
+ * - g3m3_ctx_set_cg_maxit: cap every div B / sparse_solver solve of the
+ *   context at `maxit` iterations (0 restores the reference's 10*npts,
+ *   sub_sparse_solver.f90:80); a solve that reaches the cap returns
+ *   G3M3_ERR_NOCONV, the reference's "too many iterations" warning.
+ * - g3m3_ctx_set_finite_check: when on, FP32 arrays staged from the host
+ *   (first mirror upload, g3m3_sync_to_device, g3m3_model_set_field/state,
+ *   g3m3_model_step_host) are scanned and a NaN or Inf returns
+ *   G3M3_ERR_NONFINITE before anything is uploaded.  Off by default.
+ * - g3m3_ctx_set_alloc_limit: a budget in bytes for the device memory the
+ *   context (and its models) may allocate (0: none); an allocation past it
+ *   fails with G3M3_ERR_ALLOC as a full device would.  For testing the
+ *   out-of-memory paths. g3m3_ctx_allocated gives the bytes charged so far. */
+int g3m3_ctx_set_cg_maxit(g3m3_ctx* ctx, int maxit);
+int g3m3_ctx_set_finite_check(g3m3_ctx* ctx, int on);
+int g3m3_ctx_set_alloc_limit(g3m3_ctx* ctx, size_t bytes);
+size_t g3m3_ctx_allocated(g3m3_ctx* ctx);
+
 /* ---- a1: push_ion -- sub_push_ion.f90:4-17 ---------------------------- */
 int g3m3_push_ion(g3m3_ctx* ctx,
     float* qrho, float* qpresx, float* qpresy, float* qpresz,
@@ -348,9 +367,12 @@ int g3m3_diff_fields(g3m3_ctx* ctx, int nfields, const float* const* a,
  * G3M3_NOALLOC_DIVB_MAX_CELLS cells; larger boxes are rejected with
  * G3M3_ERR_ARG.  bx, by, bz must be device (or managed) memory, else
  * G3M3_ERR_ARG; xspac and divb_band_pos may be host or device arrays.
- * The first call on each device finds the array's address there (which may
- * load the library's device code holding it): make that first call before
- * any stream capture.  Every call on a device shares the one array, which
+ * Every call looks up the array's address on the context's device.  The
+ * first call on a device may load the library's device code that holds
+ * the array (CUDA loads modules lazily), and the array's memory is taken
+ * then: make that first call at start-up, before the caller's pool claims
+ * the device and before any stream capture.  Every call on a device shares
+ * the one array, which
  * keeps the last call's contents (each call resets what the solver needs
  * zeroed); calls that overlap in time, from two threads or on two streams,
  * race on it and must be serialised by the caller. */

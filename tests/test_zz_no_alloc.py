@@ -1,12 +1,22 @@
 """g3m3_divb_correct_noalloc, the div B correction that allocates no device
 memory, against g3m3_divb_correct on the same device-resident inputs.
 
-Both run the same solver kernels; the no-allocation call keeps its solver
-state and vectors in one fixed array inside the library instead of
-per-context cudaMalloc scratch.  The comparison uses the div B parity
-tolerance of the routine tests (correction within 20 % relative L2,
-iteration counts within max(3, 25 %)).  The file name sorts last so the
-test runs after the rest of the suite as well as alone.
+Who calls it: a host code that hands the device to its own memory pool at
+start-up, or cannot take the device-wide synchronisation that cudaMalloc
+and cudaFree may bring, and so cannot let a library allocate while it runs.
+The solver state and vectors then live in one fixed array inside the
+library, shared by every call on the device.
+
+Both entries run the same solver kernels from the same zero iterate, so the
+results agree to the rounding of the FP64 atomic sums: the same iteration
+count (within one) and the correction to 1e-3 relative L2.  Calls in the
+order B, A, B, A must give each case's result twice (to 1e-5 and the same
+iteration count), which a solver started from the array's stale contents
+would not.  The first call on a device loads the array (lazily, as CUDA
+loads modules); no call after it changes the device's free memory.
+One case uses box 2 of a two-box array, so the box offset is exercised.
+The file name sorts last, so the test runs after the rest of the suite as
+well as alone.
 """
 import ctypes
 
@@ -17,16 +27,17 @@ from _support import Inputs, rel_l2
 
 pytestmark = pytest.mark.gpu
 
-CORR_TOL = 0.2
+CORR_TOL = 1e-3     # no-allocation entry vs g3m3_divb_correct
+REPEAT_TOL = 1e-5   # the same call twice
 
 
-def _case(cfg, seed, errlim):
+def _case(cfg, seed, errlim, box=1):
     I = Inputs(cfg, seed)
     p = I.p
     pos = (ctypes.c_int * 7)(p.nx * p.ny, p.nx, 1, 0, -1, -p.nx, -p.nx * p.ny)
     xs = np.array(p.xspac[: p.n_grids], np.float32)
     b = [I.cur[31].copy(), I.cur[32].copy(), I.cur[33].copy()]
-    return dict(dims=[p.nx, p.ny, p.nz, p.n_grids, 1], pos=pos, xs=xs, errlim=errlim, b=b)
+    return dict(dims=[p.nx, p.ny, p.nz, p.n_grids, box], pos=pos, xs=xs, errlim=errlim, b=b, box=box)
 
 
 def _on_device(case):
@@ -41,30 +52,56 @@ def _call(ctx, name, case, dev):
     return it.value
 
 
+def _correction(case, dev):
+    k = case["box"] - 1
+    return [dev[q].cpu().numpy()[k] - case["b"][q][k] for q in range(3)]
+
+
 def test_noalloc_matches_divb_correct_twice():
     import torch
     from g3m3_gb300.api import Context
 
-    cases = [_case("small", 11, 1e-4), _case("tiny2", 12, 1e-6)]
-    ref_dev = [_on_device(c) for c in cases]
-    new_dev = [_on_device(c) for c in cases]
+    A = _case("small", 11, 1e-4)
+    B = _case("tiny2", 12, 1e-6, box=2)
     torch.cuda.synchronize()
     with Context() as ctx:
-        ref_it = [_call(ctx, "divb_correct", c, d) for c, d in zip(cases, ref_dev)]
-        # two calls in a row; the second finds the first one's data in the array
-        it0 = _call(ctx, "divb_correct_noalloc", cases[0], new_dev[0])
-        free_before = torch.cuda.mem_get_info()[0]
-        it1 = _call(ctx, "divb_correct_noalloc", cases[1], new_dev[1])
-        free_after = torch.cuda.mem_get_info()[0]
-    assert free_after == free_before, (free_before, free_after)
-    for c, rd, nd, ri, ni in zip(cases, ref_dev, new_dev, ref_it, [it0, it1]):
+        ref = {}
+        for name, c in (("A", A), ("B", B)):
+            d = _on_device(c)
+            ref[name] = (_call(ctx, "divb_correct", c, d), _correction(c, d))
+        got = []
+        free = []
+        # the first call on the device loads the array (CUDA loads modules
+        # lazily, so the array's memory is taken there); the calls after it
+        # take nothing
+        for name, c in (("B", B), ("A", A), ("B", B), ("A", A)):
+            d = _on_device(c)
+            torch.cuda.synchronize()
+            free.append(torch.cuda.mem_get_info()[0])
+            it = _call(ctx, "divb_correct_noalloc", c, d)
+            free.append(torch.cuda.mem_get_info()[0])
+            got.append((name, it, _correction(c, d), d))
+    # no call after the first allocated device memory
+    for i in range(2, len(free), 2):
+        assert free[i + 1] == free[i], free
+    for name, it, corr, d in got:
+        c = A if name == "A" else B
+        ri, rc = ref[name]
+        assert abs(it - ri) <= 1, (name, it, ri)
         for q in range(3):
-            b0 = c["b"][q][0]
-            want = rd[q].cpu().numpy()[0] - b0
-            got = nd[q].cpu().numpy()[0] - b0
-            assert np.isfinite(got).all()
-            assert rel_l2(got, want) < CORR_TOL, (q, rel_l2(got, want), ri, ni)
-        assert abs(ni - ri) <= max(3, 0.25 * ri), (ni, ri)
+            assert np.isfinite(corr[q]).all()
+            assert rel_l2(corr[q], rc[q]) < CORR_TOL, (name, q, rel_l2(corr[q], rc[q]))
+        # the other box of a multi-box array is untouched
+        for k in range(c["dims"][3]):
+            if k != c["box"] - 1:
+                for q in range(3):
+                    assert np.array_equal(d[q].cpu().numpy()[k], c["b"][q][k])
+    # each case after the other: the same result as before it
+    for first, again in ((0, 2), (1, 3)):
+        (_, it0, c0, _), (_, it2, c2, _) = got[first], got[again]
+        assert it2 == it0, (it0, it2)
+        for q in range(3):
+            assert rel_l2(c2[q], c0[q]) < REPEAT_TOL, (q, rel_l2(c2[q], c0[q]))
 
 
 def test_noalloc_rejects_oversize_and_host_arrays():
