@@ -33,8 +33,9 @@ Semantics, chosen to match how the reference's makefile builds it
 - OpenMP directives are comments; WRITE statements are dropped.
 
 Usage: python oracle/fortran_to_c.py [reference_code_dir]
-(default <reference>/code with <reference> = $G3M3_REFERENCE or
-/root/reference).  Exits 0 without output when that directory is absent.
+(default $G3M3_REFERENCE/code; with neither, only sources translated
+earlier are compiled).  Exits 0 without output when that directory is
+absent.
 """
 from __future__ import annotations
 
@@ -1724,15 +1725,15 @@ def compile_ref(out_dir=OUT, cc="gcc", stem="g3m3_ref"):
 
 
 def reference_code_dir():
-    ref = os.environ.get("G3M3_REFERENCE", "/root/reference")
-    return os.path.join(ref, "code")
+    ref = os.environ.get("G3M3_REFERENCE")
+    return os.path.join(ref, "code") if ref else None
 
 
 def main(argv):
     code_dir = argv[1] if len(argv) > 1 else reference_code_dir()
     stems = (["g3m3_ref"] + [main_stem(t, o) for t, o in MAIN_BUILDS]
              + [main_stem(t, o, True) for t, o in R8_BUILDS])
-    if os.path.isdir(code_dir):
+    if code_dir and os.path.isdir(code_dir):
         translate(code_dir)
         for tag, omp in MAIN_BUILDS:
             translate_main(code_dir, tag, MAIN_CONFIGS[tag], omp=omp)

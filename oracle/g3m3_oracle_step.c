@@ -17,6 +17,26 @@
 static inline float amax1(float a, float b) { return a > b ? a : b; }
 static inline float amin1(float a, float b) { return a < b ? a : b; }
 
+/* The grid description (grd_*, xspac) as the routines take it: arrays of
+ * the routines' REAL type.  In the FP32 build this is an exact copy of the
+ * parameter block's arrays; the FP64 build (real8.h) widens them. */
+typedef struct {
+  float xmin[G3M3_MAX_GRIDS], xmax[G3M3_MAX_GRIDS], ymin[G3M3_MAX_GRIDS];
+  float ymax[G3M3_MAX_GRIDS], zmin[G3M3_MAX_GRIDS], zmax[G3M3_MAX_GRIDS];
+  float xspac[G3M3_MAX_GRIDS];
+} grid_reals;
+
+static grid_reals grid_of(const g3m3_params* p) {
+  grid_reals g;
+  for (int b = 0; b < G3M3_MAX_GRIDS; b++) {
+    g.xmin[b] = p->grd_xmin[b]; g.xmax[b] = p->grd_xmax[b];
+    g.ymin[b] = p->grd_ymin[b]; g.ymax[b] = p->grd_ymax[b];
+    g.zmin[b] = p->grd_zmin[b]; g.zmax[b] = p->grd_zmax[b];
+    g.xspac[b] = p->xspac[b];
+  }
+  return g;
+}
+
 /* ======================================================================
  * bndry_outer -- sub_bndry_outer.f90:5-731, applied to box n_grids.
  * The reference spells every statement out per field; the rules are the
@@ -376,18 +396,20 @@ static float set_speed_box(const g3m3_params* p, oracle_state* s,
 }
 
 static void bndry_corer_box(const g3m3_params* p, float* const f[G3M3_NFIELDS], int box) {
+  const grid_reals g = grid_of(p);
   for (int q = 0; q < G3M3_NFIELDS; q++)
-    oracle_corer(f[q], p->nx, p->ny, p->nz, p->n_grids, box, p->grd_xmin, p->grd_xmax,
-                 p->grd_ymin, p->grd_ymax, p->grd_zmin, p->grd_zmax);
+    oracle_corer(f[q], p->nx, p->ny, p->nz, p->n_grids, box, g.xmin, g.xmax,
+                 g.ymin, g.ymax, g.zmin, g.zmax);
 }
 
 static void bndry_flanks_box(const g3m3_params* p, oracle_state* s,
     float* const target[G3M3_NFIELDS], float* const cur[G3M3_NFIELDS],
     float* const old[G3M3_NFIELDS], int box, double t_grid) {
+  const grid_reals g = grid_of(p);
   for (int q = 0; q < G3M3_NFIELDS; q++)
     oracle_flanks(target[q], cur[q], old[q], p->nx, p->ny, p->nz, p->n_grids, box,
-                  s->t_new, s->t_old, t_grid, s->vv[0], p->grd_xmin, p->grd_xmax,
-                  p->grd_ymin, p->grd_ymax, p->grd_zmin, p->grd_zmax);
+                  s->t_new, s->t_old, t_grid, s->vv[0], g.xmin, g.xmax,
+                  g.ymin, g.ymax, g.zmin, g.zmax);
 }
 
 static void bndry_inner_all(const g3m3_params* p, oracle_state* s, float* const f[G3M3_NFIELDS]) {
@@ -398,6 +420,7 @@ static void bndry_inner_all(const g3m3_params* p, oracle_state* s, float* const 
 
 static void push_ions(const g3m3_params* p, oracle_state* s, float* const out[G3M3_NFIELDS],
     float* const old[G3M3_NFIELDS], float* const src[G3M3_NFIELDS], int box, float delt) {
+  const grid_reals g = grid_of(p);
   const float masses[3] = {p->rmassq, p->rmassh, p->rmasso};
   for (int sp = 0; sp < 3; sp++) {
     const int b = 10 * sp;
@@ -409,8 +432,8 @@ static void push_ions(const g3m3_params* p, oracle_state* s, float* const out[G3
                     s->bs[0], s->bs[1], s->bs[2], s->btot, s->efld[0], s->efld[1], s->efld[2],
                     masses[sp], s->vv[0], s->vv[1], s->vv[2], s->tv[0], s->tv[1], s->tv[2],
                     p->gamma, p->gamma1, p->nx, p->ny, p->nz, p->n_grids, box, delt, p->grav,
-                    p->re_equiv, p->reynolds, p->grd_xmin, p->grd_xmax, p->grd_ymin,
-                    p->grd_ymax, p->grd_zmin, p->grd_zmax, p->isotropic);
+                    p->re_equiv, p->reynolds, g.xmin, g.xmax, g.ymin,
+                    g.ymax, g.zmin, g.zmax, p->isotropic);
   }
 }
 
@@ -625,16 +648,17 @@ int oracle_main_step(const g3m3_params* p, oracle_state* s) {
 }
 
 void oracle_divb_all(const g3m3_params* p, oracle_state* s) {
+  const grid_reals g = grid_of(p);
   const int nx = p->nx, ny = p->ny, ng = p->n_grids;
   const int pos[7] = {nx * ny, nx, 1, 0, -1, -nx, -nx * ny};
   for (int box = ng; box >= 1; box--) {
     for (int rep = 0; rep < 2; rep++)
-      s->last_cg_iters = oracle_divb_correct(nx, ny, p->nz, ng, box, 7, pos, p->xspac,
+      s->last_cg_iters = oracle_divb_correct(nx, ny, p->nz, ng, box, 7, pos, g.xspac,
           p->divb_errlim, s->cur[G3M3_F_BX], s->cur[G3M3_F_BY], s->cur[G3M3_F_BZ]);
   }
   for (int box = ng - 1; box >= 1; box--)
     for (int q = G3M3_F_BX; q <= G3M3_F_BZ; q++)
-      oracle_flanks_synced(s->cur[q], nx, ny, p->nz, ng, box, p->grd_xmin, p->grd_xmax,
-                           p->grd_ymin, p->grd_ymax, p->grd_zmin, p->grd_zmax);
+      oracle_flanks_synced(s->cur[q], nx, ny, p->nz, ng, box, g.xmin, g.xmax,
+                           g.ymin, g.ymax, g.zmin, g.zmax);
   for (int box = 1; box <= ng - 1; box++) bndry_corer_box(p, s->cur, box);
 }

@@ -30,6 +30,12 @@ def fptr(a):
     return a.ctypes.data_as(_fp)
 
 
+def _rptr(a):
+    """A float64 array passed where the FP64 build's REAL pointers go."""
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"], (a.dtype, a.flags)
+    return ctypes.cast(a.ctypes.data, _fp)
+
+
 def iptr(a):
     assert a.dtype == np.int32 and a.flags["C_CONTIGUOUS"]
     return a.ctypes.data_as(_ip)
@@ -56,13 +62,16 @@ class OracleState(ctypes.Structure):
 _LIBS = {}
 
 
-def lib(omp: bool = False):
-    name = "liboracle_omp.so" if omp else "liboracle.so"
+def lib(omp: bool = False, real8: bool = False):
+    name = "liboracle" + ("_r8" if real8 else "") + ("_omp" if omp else "") + ".so"
     if name not in _LIBS:
         path = os.path.join(HERE, name)
         if not os.path.exists(path):
             build()
         L = ctypes.CDLL(path)
+        if real8:   # only the main-step entries (below) are used; their arguments are pointers
+            _LIBS[name] = L
+            return L
         from g3m3_gb300 import _lib as glib
         for fname, ret, params in glib.header_functions(os.path.join(HERE, "g3m3_oracle.h"), "oracle_"):
             fn = getattr(L, fname)
@@ -74,20 +83,28 @@ def lib(omp: bool = False):
 
 class OracleModel:
     """Holds a full multi-box state in numpy arrays and steps it on the CPU
-    with the oracle's restatement of the reference main loop."""
+    with the oracle's restatement of the reference main loop.  With
+    ``real8``, the FP64 build (every REAL in double precision, real8.h):
+    the state is float64, started from the FP32 state's values."""
 
-    def __init__(self, state, omp: bool = False):
-        self.L = lib(omp)
+    def __init__(self, state, omp: bool = False, real8: bool = False):
+        self.L = lib(omp, real8)
+        self.real8 = real8
         self.p = state.params
         p = self.p
-        self.cur = state.cur.copy()
+        ft = np.float64 if real8 else np.float32
+        self.cur = state.cur.astype(ft)
         self.old = np.zeros_like(self.cur)
         self.wrk = self.cur.copy()   # wrkepres is read before it is written
-        self.b0 = state.b0.copy()
-        self.resistive = state.resistive.copy()
+        self.b0 = state.b0.astype(ft)
+        self.resistive = state.resistive.astype(ft)
         self.lists = {k: np.ascontiguousarray(v) for k, v in state.lists.items()}
+        if real8:
+            for k in ("parm_srf", "parm_mid", "parm_zero"):
+                self.lists[k] = np.ascontiguousarray(self.lists[k], np.float64)
         box = (p.nz, p.ny, p.nx)
-        self.scr = np.zeros((19,) + box, np.float32)
+        self.scr = np.zeros((19,) + box, ft)
+        fptr = _rptr if real8 else globals()["fptr"]
         s = OracleState()
         for q in range(NFIELDS):
             s.cur[q] = fptr(self.cur[q]); s.old[q] = fptr(self.old[q]); s.wrk[q] = fptr(self.wrk[q])

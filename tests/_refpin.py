@@ -37,8 +37,9 @@ def load():
         if ROOT not in sys.path:
             sys.path.insert(0, ROOT)
         from oracle import fortran_to_c
+        import __graft_entry__
         try:
-            fortran_to_c.main(["fortran_to_c"])
+            fortran_to_c.main(["fortran_to_c", os.path.join(__graft_entry__.REFERENCE, "code")])
         except Exception:
             return None
     if not os.path.exists(so):
