@@ -1,0 +1,178 @@
+"""Gradients of a virtual-spacecraft misfit through the step engine
+(g3m3_adjoint_* of libg3m3_gpu.so), and their torch.autograd binding.
+
+``Adjoint`` wraps the C ABI: a forward run of N main steps from a model's
+state (time steps recorded, state checkpointed every K steps, the misfit of
+samples taken at the end of their main steps), then the hand-written
+reverse of every kernel, checkpoint segment by checkpoint segment, which
+gives dL/d(upstream parameters of the wind face) and dL/d(state before the
+first step).
+
+``upstream_wind`` maps the physical upstream conditions (n in cm^-3,
+v in km/s, IMF in nT; 3d_main.f90:907-943) to the eight wind-face
+parameters as torch operations, and ``WindMisfit`` is a
+torch.autograd.Function of those eight parameters whose backward is the
+CUDA adjoint, so
+
+    loss = WindMisfit.apply(upstream_wind(u, setup), run)
+    loss.backward()            # u.grad = dL/d(n, vx, vy, vz, bx, by, bz)
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+
+from .api import Model, addr
+from .params import NFIELDS
+
+WIND = ("srho", "spx", "spy", "spz", "spress", "sbx_wind", "sby_wind", "sbz_wind")
+
+# physical constants of the unit conversions (3d_main.f90:907-943)
+MU0 = 4.0e-7 * math.pi
+M_PROT = 1.6726e-27
+EV = 1.6022e-19
+
+
+class Adjoint:
+    def __init__(self, model: Model, nsteps: int, checkpoint_every: int = 10, cg_errlim: float = 0.0):
+        self.model = model
+        self.L = model.L
+        self.ctx = model.ctx
+        self.nsteps = int(nsteps)
+        h = ctypes.c_void_p()
+        self.ctx.check(self.L.g3m3_adjoint_create(model.h, self.nsteps, int(checkpoint_every), float(cg_errlim),
+                                                  ctypes.byref(h)))
+        self.h = h
+        self._keep = []
+        self.ctx._models.insert(0, self)   # closed before the models when the context closes
+
+    def set_samples(self, xyz, step, target):
+        """xyz (n, 3) planet radii; step (n,) main step (1-based) at whose end
+        the sample is taken, non-decreasing; target (n, 4): bx, by, bz, rho."""
+        xyz = np.ascontiguousarray(xyz, np.float32)
+        step = np.ascontiguousarray(step, np.int32)
+        target = np.ascontiguousarray(target, np.float32)
+        self.ctx.check(self.L.g3m3_adjoint_set_samples(self.h, int(len(step)), addr(xyz), addr(step), addr(target)))
+
+    def forward(self, schedule=None):
+        """Run the N main steps from the model's state; returns the misfit.
+        With ``schedule`` ((N, n_grids) t_stepnew), the time steps are those."""
+        loss = ctypes.c_double()
+        sch = None
+        if schedule is not None:
+            sch = np.ascontiguousarray(schedule, np.float64)
+            self._keep = [sch]
+        self.ctx.check(self.L.g3m3_adjoint_forward(self.h, addr(sch) if sch is not None else None,
+                                                   ctypes.byref(loss)))
+        return loss.value
+
+    def schedule(self):
+        out = np.empty((self.nsteps, self.model.p.n_grids), np.float64)
+        self.ctx.check(self.L.g3m3_adjoint_schedule(self.h, addr(out)))
+        return out
+
+    def backward(self, state=True):
+        """dL/d(wind parameters) (8, float64), and with ``state`` dL/d(state
+        before the first step) (34, n_grids, nz, ny, nx) and dL/d(wrk epres)."""
+        p = self.model.p
+        gp = np.zeros(8, np.float64)
+        gs = np.zeros((NFIELDS, p.n_grids, p.nz, p.ny, p.nx), np.float32) if state else None
+        gw = np.zeros((p.n_grids, p.nz, p.ny, p.nx), np.float32) if state else None
+        rc = self.L.g3m3_adjoint_backward(self.h, addr(gp), addr(gs) if state else None, addr(gw) if state else None)
+        if rc not in (0, 3):   # 3: an adjoint div B solve hit its iteration cap (a warning)
+            self.ctx.check(rc)
+        return dict(params=gp, state=gs, wrk_epres=gw, noconv=rc == 3)
+
+    def tape_bytes(self):
+        return int(self.L.g3m3_adjoint_tape_bytes(self.h))
+
+    def close(self):
+        if self.h and self.model.h and self.ctx.h:
+            self.L.g3m3_adjoint_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def wind_scales(setup):
+    """Constants of the upstream conversion for a state.Setup: (1/rho_equiv *
+    rmassq, 1/v_equiv, spress per unit srho, 1/b_equiv)."""
+    gamma = 5.0 / 3.0
+    b_equiv = setup.v_equiv * 1.0e3 * math.sqrt(MU0 * setup.rho_equiv * 1.0e6 * M_PROT) * 1.0e9
+    cs_wind = math.sqrt(gamma * setup.wind.t_ev * EV / M_PROT) / 1.0e3 / setup.v_equiv
+    return setup.rmassq / setup.rho_equiv, 1.0 / setup.v_equiv, (cs_wind ** 2 / gamma) / (gamma - 1.0), 1.0 / b_equiv
+
+
+def upstream_wind(u, setup):
+    """The eight wind-face parameters from u = (n [cm^-3], vx, vy, vz [km/s],
+    bx, by, bz [nT]) as torch operations (differentiable): srho = n m_q /
+    rho_equiv, sp = srho v / v_equiv, spress = srho cs^2 / (gamma (gamma-1)),
+    sb = B / b_equiv (state.py's conversion with the temperature held)."""
+    import torch
+    kr, kv, kp, kb = wind_scales(setup)
+    srho = u[0] * kr
+    return torch.stack([srho, srho * u[1] * kv, srho * u[2] * kv, srho * u[3] * kv, srho * kp,
+                        u[4] * kb, u[5] * kb, u[6] * kb])
+
+
+class MisfitRun:
+    """A fixed experiment: the model's initial state, N main steps, the
+    samples and (after the first call) the time-step schedule; ``loss(w)``
+    runs it with wind parameters w and keeps the adjoint ready."""
+
+    def __init__(self, model: Model, state, nsteps, samples, checkpoint_every=10, cg_errlim=0.0, schedule=None):
+        self.model = model
+        self.state = state
+        self.adj = Adjoint(model, nsteps, checkpoint_every, cg_errlim)
+        self.adj.set_samples(*samples)
+        self.schedule = schedule
+
+    def reset(self):
+        self.model.upload(self.state)
+        self.model.init_steps()
+
+    def loss(self, wind):
+        w = np.ascontiguousarray(np.asarray(wind, np.float64).astype(np.float32))
+        self.model.ctx.check(self.model.L.g3m3_model_set_wind(self.model.h, addr(w)))
+        self.reset()
+        val = self.adj.forward(self.schedule)
+        if self.schedule is None:
+            self.schedule = self.adj.schedule()
+        return val
+
+
+def _function():
+    import torch
+
+    class WindMisfit(torch.autograd.Function):
+        """loss = misfit of a MisfitRun with the given wind parameters (8);
+        backward: the hand-written CUDA adjoint."""
+
+        @staticmethod
+        def forward(ctx, wind, run):
+            ctx.run = run
+            val = run.loss(wind.detach().cpu().numpy())
+            return torch.tensor(val, dtype=torch.float64)
+
+        @staticmethod
+        def backward(ctx, g):
+            grads = ctx.run.adj.backward(state=False)
+            return torch.from_numpy(grads["params"]) * g, None
+
+    return WindMisfit
+
+
+class _Lazy:
+    fn = None
+
+
+def WindMisfit():
+    if _Lazy.fn is None:
+        _Lazy.fn = _function()
+    return _Lazy.fn

@@ -23,7 +23,7 @@
 
 #include <nvtx3/nvToolsExt.h>
 
-#include "ctx.cuh"
+#include "model.cuh"
 
 namespace g3m3 {
 int run_divb(g3m3_ctx* c, float* bx, float* by, float* bz, const Dims& d, float rx, float errlim, CgState* st,
@@ -58,82 +58,6 @@ const char* const kBoxStepRange[8] = {"box-step 1", "box-step 2", "box-step 3", 
 
 }  // namespace
 
-struct g3m3_model {
-  g3m3_ctx* ctx = nullptr;
-  cudaStream_t stream = nullptr;     // the context's stream, or the member's own in an ensemble
-  bool own_stream = false;
-  cudaStream_t aux[3] = {};          // side streams for independent kernels of a stage
-  cudaEvent_t fork_ev = nullptr, join_ev[3] = {};
-  g3m3_params p{};
-  Dims d{};
-  size_t n3 = 0, n4 = 0;
-  float* mem = nullptr;              // one allocation for every array below
-  float* buf[3][G3M3_NFIELDS] = {};  // three full (nx,ny,nz,n_grids) copies per field
-  int role_cur[G3M3_MAX_GRIDS] = {}, role_old[G3M3_MAX_GRIDS] = {};
-  float* b0[3] = {};
-  float* resistive = nullptr;
-  float* rst_e = nullptr;            // BandE's resistive coefficient per cell (0: none)
-  bool lists_unique = true;
-  int* ij[3] = {};
-  float* parm[3] = {};
-  int num[3][G3M3_MAX_GRIDS] = {};
-  int mlen[3] = {};
-  bool inner_set = false;
-  bool inner_in_shell = true;        // an inner-boundary cell lies in the two-cell flank shell
-  float *efld[3], *curr[3], *bs[3], *btot, *ev[3], *tv[3], *vt[3];
-  float* glist = nullptr;
-  float* flank_ibuf = nullptr;       // interpolated flank values of a box-step [field][shell cell]
-  size_t gcap = 0;
-  unsigned* words = nullptr;         // [0] list count, [1..5] maxima scratch, [8+5b..] per-box maxima
-  unsigned* host_words = nullptr;
-  CgState* cg = nullptr;
-  CgState* host_cg = nullptr;
-  float* cgvec = nullptr;
-  // div B of all boxes at once: per-box solver state, vectors (box 1 uses
-  // cgvec) and streams, made at the first pass
-  CgState* cg_box = nullptr;
-  CgState* host_cg_box = nullptr;
-  float* cgvec_more = nullptr;
-  cudaStream_t divb_stream[G3M3_MAX_GRIDS] = {};
-  cudaEvent_t divb_ev[G3M3_MAX_GRIDS] = {};
-  int cg_hint_box[G3M3_MAX_GRIDS] = {};
-  CgRun divb_run[G3M3_MAX_GRIDS];      // the pass in flight (divb_begin / divb_poll / divb_end)
-  int divb_rep[G3M3_MAX_GRIDS] = {};
-  bool divb_fin[G3M3_MAX_GRIDS] = {};
-  int divb_worst = 0;
-  // host-fed step (g3m3_model_step_host): the state to upload while the
-  // next step is enqueued, box by box on a copy stream
-  const float* up_src = nullptr;
-  bool up_waited[G3M3_MAX_GRIDS] = {};
-  cudaStream_t copy_stream = nullptr;
-  cudaEvent_t up_fork = nullptr, up_ev[G3M3_MAX_GRIDS] = {};
-  float* d_scal = nullptr;
-  float* h_scal = nullptr;
-  int nscal = 0, scal_cap = 0;
-  double t = 0.0;
-  double t_old[G3M3_MAX_GRIDS] = {}, t_new[G3M3_MAX_GRIDS] = {};
-  double t_step[G3M3_MAX_GRIDS] = {}, t_stepnew[G3M3_MAX_GRIDS] = {};
-  int64_t cell_updates = 0;
-  int nsteps_done = 0;
-  float iso_flag = 1.0f;
-  int64_t kernels = 0, graph_launches = 0;
-  std::vector<int> h_ij[3];          // host copies of the inner-boundary tables (fluid files)
-  std::vector<float> h_parm[3];
-  int fcs_variant = 0;               // fcsmooth tile shape (g3m3_model_autotune)
-  float* flux_hist = nullptr;        // flux_counter history [step][box][6]
-  unsigned* flux_count = nullptr;
-  int flux_cap = 0;
-  float flux_scale[G3M3_MAX_GRIDS] = {};
-  float* craft_traj = nullptr;       // virtual spacecraft: trajectories (4, samples)
-  int* craft_start = nullptr;        // first sample of each craft
-  float* craft_out = nullptr;        // records [step][craft][4 + nf]
-  unsigned* craft_count = nullptr;
-  int ncraft = 0, craft_nf = 0, craft_cap = 0, craft_t_slot = -1;
-  int craft_fields[8] = {};
-  std::map<std::string, cudaGraphExec_t> graphs;
-  std::map<std::string, int64_t> kernel_nodes;
-  int64_t launches_in_step = 0;
-};
 
 namespace {
 
@@ -411,6 +335,10 @@ int plan_main_step(g3m3_model* m, std::vector<Action>& acts) {
   const int ng = p.n_grids;
   acts.clear();
   m->nscal = 0;
+  if (m->forced_steps && m->forced_i < m->forced_n) {   // a prescribed schedule (the adjoint's fixed dt)
+    for (int b = 0; b < ng; b++) m->t_stepnew[b] = m->forced_steps[(size_t)m->forced_i * ng + b];
+    m->forced_i++;
+  }
   double smallest_step = 0.0;
   int m_smallest = ng;
   for (int box = ng; box >= 1; box--) {
@@ -505,12 +433,52 @@ void apply_role_swaps(g3m3_model* m, const std::vector<Action>& acts) {
     if (a.kind == Action::BOX_STEP) std::swap(m->role_cur[a.box - 1], m->role_old[a.box - 1]);
 }
 
+// The fields stage (calcur, bs/btot, fnd_evel, BandE into the model's
+// scratch) and fnd_vtot of an explicit field table, for the adjoint's
+// recomputation of primal values.
+thread_local float* const* tl_table = nullptr;
+float* table_get(g3m3_model*, int f, int) { return tl_table[f]; }
+
+}  // namespace
+
+namespace g3m3 {
+void engine_fields(g3m3_model* m, float* const f[G3M3_NFIELDS], int b) {
+  tl_table = f;
+  fields_stage(m, table_get, b);
+  tl_table = nullptr;
+}
+
+void engine_vtot(g3m3_model* m, float* const f[G3M3_NFIELDS]) {
+  VtotArgs va{};
+  for (int s = 0; s < 3; s++) {
+    for (int q = 0; q < 3; q++) va.p[s][q] = f[10 * s + 1 + q];
+    va.rho[s] = f[10 * s];
+  }
+  for (int q = 0; q < 3; q++) va.v[q] = m->vt[q];
+  va.d = m->d;
+  launch_vtot(va, S(m));
+}
+}  // namespace g3m3
+
+namespace {
+
+// The tape's snapshot of state `get` of box b at `point` (adjoint recording).
+void snap(g3m3_model* m, int point, Getter get, int b) {
+  if (!m->tape) return;
+  float* f[G3M3_NFIELDS];
+  for (int q = 0; q < G3M3_NFIELDS; q++) f[q] = get(m, q, b);
+  tape_snap(m, point, b, f);
+}
+
 // Launch the kernels of one box-step (predictor, corrector, Lapidus, flux
 // correction, each followed by boundaries and guards; 3d_main.f90:2170-3039).
 int enqueue_box_step(g3m3_model* m, const Action& act) {
   const g3m3_params& p = m->p;
   const int ng = p.n_grids, b = act.box;
   Range box_range(kBoxStepRange[b - 1 < 8 ? b - 1 : 7]);
+  if (m->tape)
+    tape_box_start(m, b, m->h_scal[act.s_half], m->h_scal[act.s_full], act.s_t1p >= 0 ? m->h_scal[act.s_t1p] : 0.0f,
+                   act.s_t1c >= 0 ? m->h_scal[act.s_t1c] : 0.0f);
   std::swap(m->role_cur[b - 1], m->role_old[b - 1]);   // store_array
   int st;
   {
@@ -519,7 +487,9 @@ int enqueue_box_step(g3m3_model* m, const Action& act) {
     fields_stage(m, O, b);
     push_stage(m, W, O, b, act.s_half, false);
     boundary_stage(m, W, b, act.s_t1p);
+    snap(m, TP_PRED_BNDRY, W, b);
     if ((st = guard_stage(m, W, b, true, false))) return st;
+    snap(m, TP_PRED_GUARD, W, b);
   }
   {
     Range r("corrector");
@@ -535,7 +505,9 @@ int enqueue_box_step(g3m3_model* m, const Action& act) {
       // stages, which use the same time weight.
       boundary_stage(m, W, b, act.s_t1c, C, FLANKS_KEEP);
     }
+    snap(m, TP_CORR_BNDRY, C, b);
     if ((st = guard_stage(m, C, b, true, false))) return st;
+    snap(m, TP_CORR_GUARD, C, b);
   }
   {
     // Lapidus smoothing (3d_main.f90:2690-2772): the three species beside
@@ -578,7 +550,9 @@ int enqueue_box_step(g3m3_model* m, const Action& act) {
     join_aux(m);
     m->launches_in_step += 5;
     boundary_stage(m, W, b, act.s_t1c, nullptr, FLANKS_REUSE);
+    snap(m, TP_LAP_BNDRY, W, b);
     if ((st = guard_stage(m, W, b, true, false))) return st;
+    snap(m, TP_LAP_GUARD, W, b);
   }
   // flux correction (3d_main.f90:2896-3036)
   Range r("flux_correct");
@@ -593,6 +567,7 @@ int enqueue_box_step(g3m3_model* m, const Action& act) {
   launch_fcsmooth(fa, S(m));
   m->launches_in_step += 1;
   boundary_stage(m, C, b, act.s_t1c, nullptr, FLANKS_REUSE);
+  snap(m, TP_FCS_BNDRY, C, b);
   return guard_stage(m, C, b, true, true);
 }
 
@@ -614,9 +589,13 @@ int enqueue_plan(g3m3_model* m, const std::vector<Action>& acts) {
     if (a.box <= m->p.mbndry && (st = upload_wait(m, m->p.mbndry))) return st;
     switch (a.kind) {
       case Action::BOX_STEP: st = enqueue_box_step(m, a); break;
-      case Action::CORE_SYNC: corer_stage(m, a.box); break;
+      case Action::CORE_SYNC:
+        if (m->tape) tape_core(m, a.box);
+        corer_stage(m, a.box);
+        break;
       case Action::FINAL_SYNC:
         corer_stage(m, a.box);
+        if (m->tape) tape_final(m, a.box);
         st = guard_stage(m, C, a.box, false, false);
         break;
     }
@@ -929,6 +908,17 @@ int g3m3_model_get_state(g3m3_model* m, float* data) {
   return e == cudaSuccess ? G3M3_OK : cuda_check(m->ctx, e, "get_state sync");
 }
 
+int g3m3_model_set_wind(g3m3_model* m, const float* wind) {
+  if (!m || !wind) return G3M3_ERR_ARG;
+  m->p.srho = wind[0]; m->p.spx = wind[1]; m->p.spy = wind[2]; m->p.spz = wind[3];
+  m->p.spress = wind[4]; m->p.sbx_wind = wind[5]; m->p.sby_wind = wind[6]; m->p.sbz_wind = wind[7];
+  // captured step graphs hold the old values in their bndry_outer launches
+  for (auto& kv : m->graphs) cudaGraphExecDestroy(kv.second);
+  m->graphs.clear();
+  m->kernel_nodes.clear();
+  return G3M3_OK;
+}
+
 int g3m3_model_set_b0(g3m3_model* m, const float* bx0, const float* by0, const float* bz0) {
   if (!m || !bx0 || !by0 || !bz0) return G3M3_ERR_ARG;
   const float* s[3] = {bx0, by0, bz0};
@@ -1150,6 +1140,7 @@ int divb_end(g3m3_model* m) {
 int g3m3_model_divb_all(g3m3_model* m) {
   if (!m) return G3M3_ERR_ARG;
   Range range("div B pass");
+  if (m->tape) tape_divb(m);
   int st = divb_begin(m);
   for (bool done = false; !st && !done;) st = divb_poll(m, &done);
   return st ? st : divb_end(m);

@@ -382,6 +382,48 @@ int g3m3_divb_correct_noalloc(g3m3_ctx* ctx, int nx, int ny, int nz,
     const float* xspac, float divb_errlim, float* bx, float* by, float* bz,
     int* iters);
 
+/* ---- the adjoint of the main steps (no counterpart in the reference) ----
+ * Gradients of a virtual-spacecraft misfit
+ *   L = sum over samples of sum_q (value_q(x_s) - target_q,s)^2,
+ *   q = bx, by, bz (the perturbation field) and the total density
+ *   qrho + hrho + orho, trilinear in the smallest box holding x_s
+ *   (findgrid cft_findgrid.f90:70-126, trilin_interp cft_trilin_interp.f90:
+ *   34-54), each sample taken at the end of its main step,
+ * with respect to the eight upstream parameters of bndry_outer's wind face
+ * (sub_bndry_outer.f90:50-103: srho, spx, spy, spz, spress, sbx_wind,
+ * sby_wind, sbz_wind) and to the model's state before the first step.
+ * g3m3_adjoint_forward runs nsteps main steps from the model's state
+ * (host-launched; the schedule of time steps recorded, or the one given;
+ * the state kept every checkpoint_every steps) and returns L.
+ * g3m3_adjoint_backward restores each checkpoint, re-runs its steps under
+ * the recorded schedule with the snapshots the reverse needs, and runs the
+ * hand-written reverse of every kernel backwards; it returns dL/dparams
+ * (8 doubles), dL/dstate ((34, n_grids, nz, ny, nx) floats, host or
+ * device) and dL/d(wrk epres) (the one wrk field the first step reads),
+ * and leaves the model at the end of the run.  The time steps are held
+ * fixed; the div B solves are reversed as exact linear solves with the
+ * forward's CG at cg_errlim (0: the model's divb_errlim); a reversed solve
+ * that hits the iteration cap makes backward return G3M3_ERR_NOCONV after
+ * finishing.  Requires mbndry = 1 and inner-boundary lists of distinct
+ * cells.  Device memory: the checkpoints, and for the steps of one
+ * checkpoint interval 8 snapshots of 34 fields per box-step
+ * (g3m3_adjoint_tape_bytes). */
+typedef struct g3m3_adjoint g3m3_adjoint;
+int g3m3_adjoint_create(g3m3_model* m, int nsteps, int checkpoint_every,
+    float cg_errlim, g3m3_adjoint** out);
+int g3m3_adjoint_destroy(g3m3_adjoint* a);
+/* n samples: xyz(3,n) in planet radii, step(n) in 1..nsteps non-decreasing,
+ * target(4,n) = bx, by, bz, rho */
+int g3m3_adjoint_set_samples(g3m3_adjoint* a, int n, const float* xyz,
+    const int* step, const float* target);
+int g3m3_adjoint_forward(g3m3_adjoint* a, const double* schedule, double* loss);
+/* the recorded schedule: t_stepnew of every box before each main step,
+ * (nsteps, n_grids) doubles, for g3m3_adjoint_forward of another run */
+int g3m3_adjoint_schedule(g3m3_adjoint* a, double* out);
+int g3m3_adjoint_backward(g3m3_adjoint* a, double* grad_params,
+    float* grad_state, float* grad_wrk_epres);
+size_t g3m3_adjoint_tape_bytes(g3m3_adjoint* a);
+
 /* ---- a19: virtual spacecraft -- findgrid cft_findgrid.f90:4 and
  * trilin_interp cft_trilin_interp.f90:10, batched over n trajectory points:
  * xyz(3,n) in planet radii; out(n) = trilinear value of field at each point
@@ -407,6 +449,10 @@ int g3m3_model_get_field(g3m3_model* m, int which, int field, float* data);
 int g3m3_model_set_state(g3m3_model* m, const float* data);
 int g3m3_model_get_state(g3m3_model* m, float* data);
 int g3m3_model_set_b0(g3m3_model* m, const float* bx0, const float* by0, const float* bz0);
+/* The upstream parameters of bndry_outer's wind face (sub_bndry_outer.f90:
+ * 50-103), 8 floats: srho, spx, spy, spz, spress, sbx_wind, sby_wind,
+ * sbz_wind; the next main step uses them. */
+int g3m3_model_set_wind(g3m3_model* m, const float* wind);
 int g3m3_model_set_inner(g3m3_model* m, const float* resistive,
     const int* ijsrf, const int* numsrf, const float* parm_srf, int msrf,
     const int* ijmid, const int* nummid, const float* parm_mid, int mmid,

@@ -77,3 +77,28 @@ def check(res):
             if not eg <= SLACK * er + FLOOR:
                 bad.append((n, name, eg, er))
     return bad
+
+
+def divb_correct_r8(nx, ny, nz, n_grids, box, pos, xspac, errlim, bx, by, bz):
+    """oracle_divb_correct of the FP64 build on float64 copies of bx, by, bz
+    (returned, with the iteration count)."""
+    import ctypes
+    from oracle.oracle import lib
+    L = lib(real8=True)
+    fn = L.oracle_divb_correct
+    fn.restype = ctypes.c_int
+    b = [np.ascontiguousarray(x, np.float64).copy() for x in (bx, by, bz)]
+    xs = np.ascontiguousarray(xspac, np.float64)
+    vp = ctypes.c_void_p
+    fn.argtypes = [ctypes.c_int] * 6 + [vp, vp, ctypes.c_double, vp, vp, vp]
+    it = fn(nx, ny, nz, n_grids, box, 7, ctypes.addressof(pos), xs.ctypes.data, float(errlim),
+            b[0].ctypes.data, b[1].ctypes.data, b[2].ctypes.data)
+    return b, it
+
+
+def divb_all_r8(state):
+    """The div B pass of every box (divb_all) in the FP64 build: float64 state."""
+    from oracle.oracle import OracleModel
+    om = OracleModel(state, real8=True)
+    om.divb_all()
+    return om.cur

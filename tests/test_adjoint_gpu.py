@@ -1,0 +1,91 @@
+"""The hand-written adjoint of the main steps (g3m3_adjoint_*) against FP64
+central differences of the same run.
+
+The misfit of virtual-spacecraft samples along a straight line through the
+outermost box, taken at the end of their main steps; its gradient with
+respect to the eight wind-face parameters of bndry_outer and to the state
+before the first step, from the library's FP32 forward and reverse kernels,
+checked against central differences of the oracle's FP64 build run under
+the same time-step schedule (tests/_adjoint_ref.py).  h = 1e-4 relative to
+each parameter's scale.
+"""
+import numpy as np
+import pytest
+
+import _adjoint_ref as R
+
+pytestmark = pytest.mark.gpu
+
+GRAD_TOL = 1e-3
+
+
+def _run(cfg, nsteps, every, nsamp=40, **over):
+    from g3m3_gb300.adjoint import MisfitRun
+    from g3m3_gb300.api import Context, Model
+    from g3m3_gb300.state import make_config
+    st = make_config(cfg, **over)
+    samples = R.line_samples(st, nsteps, n=nsamp)
+    ctx = Context()
+    m = Model(ctx, st)
+    run = MisfitRun(m, st, nsteps, samples, checkpoint_every=every)
+    return ctx, st, samples, run
+
+
+def _fd_params(st, sch, samples, w, idx):
+    scale = [abs(w[0]), abs(w[1]), abs(w[1]), abs(w[1]), abs(w[4]), abs(w[7]) + abs(w[6]),
+             abs(w[7]) + abs(w[6]), abs(w[7]) + abs(w[6])]
+    g = np.zeros(8)
+    for k in idx:
+        h = 1e-4 * scale[k]
+        wp, wm = w.copy(), w.copy()
+        wp[k] += h
+        wm[k] -= h
+        g[k] = (R.oracle_loss(st, wp, sch, samples) - R.oracle_loss(st, wm, sch, samples)) / (2 * h)
+    return g
+
+
+@pytest.mark.parametrize("cfg,nsteps,every,divb", [("tiny3", 4, 2, 0), ("tiny3", 4, 4, 2)])
+def test_wind_gradient_against_fp64_differences(cfg, nsteps, every, divb):
+    over = dict(divb_every=divb, divb_errlim=1e-6) if divb else dict(divb_every=0)
+    ctx, st, samples, run = _run(cfg, nsteps, every, **over)
+    w = R.wind_of(st)
+    loss = run.loss(w)
+    sch = run.schedule
+    grads = run.adj.backward()
+    ctx.close()
+    l64 = R.oracle_loss(st, w, sch, samples)
+    assert abs(loss - l64) <= 1e-4 * abs(l64), (loss, l64)
+    fd = _fd_params(st, sch, samples, w, range(8))
+    ga = grads["params"]
+    print("adjoint", ga)
+    print("fd     ", fd)
+    err = np.linalg.norm(ga - fd) / np.linalg.norm(fd)
+    assert err <= GRAD_TOL, (err, ga, fd)
+
+
+def test_state_gradient_directional():
+    ctx, st, samples, run = _run("tiny3", 3, 1, divb_every=0)
+    w = R.wind_of(st)
+    run.loss(w)
+    sch = run.schedule
+    grads = run.adj.backward()
+    ctx.close()
+    rng = np.random.default_rng(11)
+    scale = np.abs(st.cur).reshape(34, -1).mean(axis=1)
+    delta = np.stack([scale[q] * rng.standard_normal(st.cur.shape[1:]) for q in range(34)])
+    h = 1e-4
+    fd = (R.oracle_loss(st, w, sch, samples, delta=h * delta) - R.oracle_loss(st, w, sch, samples,
+                                                                               delta=-h * delta)) / (2 * h)
+    ad = float((grads["state"].astype(np.float64) * delta).sum())
+    print("directional adjoint", ad, "fd", fd)
+    assert abs(ad - fd) <= GRAD_TOL * abs(fd), (ad, fd)
+
+
+def test_checkpoint_interval_does_not_change_the_gradient():
+    out = []
+    for every in (1, 3):
+        ctx, st, samples, run = _run("tiny3", 3, every, divb_every=0)
+        run.loss(R.wind_of(st))
+        out.append(run.adj.backward()["params"])
+        ctx.close()
+    assert np.allclose(out[0], out[1], rtol=1e-5, atol=1e-9 * np.abs(out[0]).max()), out

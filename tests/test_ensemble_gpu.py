@@ -106,3 +106,30 @@ def test_ensemble_autotune_per_box_size():
             assert om.main_step() == 0
         for q in range(34):
             assert_same(g[q], om.cur[q], f"member field {q}")
+
+
+def test_ensemble_bench_sizes_one_step():
+    """The bench's ensemble shapes: three members of five nested boxes of
+    121x121x61, 97x97x49 and 81x81x41 with upstream conditions drawn from
+    the seed, the flux-correction forms the autotuner picks for those sizes
+    (7, 5, 7), one main step in one CUDA graph: every member's 34 fields are
+    the oracle's bits."""
+    from g3m3_gb300.api import Context, Ensemble
+    from g3m3_gb300.state import ensemble_member
+    from oracle.oracle import OracleModel
+    states = [ensemble_member(i) for i in range(3)]
+    assert [s.params.nx for s in states] == [121, 97, 81]
+    with Context() as ctx:
+        ens = Ensemble(ctx, states)
+        for m, v in zip(ens.members, (7, 5, 7)):
+            m.set_variant(1, v)
+        ens.init_steps()
+        ens.run(1, graph=True)
+        outs = [m.state() for m in ens.members]
+        ens.close()
+    for i, (st, out) in enumerate(zip(states, outs)):
+        om = OracleModel(st, omp=True)
+        om.init_steps()
+        assert om.main_step() == 0
+        for q in range(34):
+            assert_same(out[q], om.cur[q], f"member {i} field {q}")

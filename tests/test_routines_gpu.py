@@ -297,8 +297,9 @@ def divergence(bx, by, bz, rx):
 
 @pytest.mark.parametrize("cfg,errlim", [("tiny2", 1e-4), ("tiny2", 1e-6), ("small", 1e-4)])
 def test_divb_correct(cfg, errlim):
-    """Compared at the solver's tolerance: the oracle sums dot products
-    serially in FP32 as the reference does, the library in FP64."""
+    """Compared with the FP64 build: the oracle sums dot products serially
+    in FP32 as the reference does, the library in FP64; the library's B must
+    be as close to the FP64 solve as the reference's (tests/_divb_parity.py)."""
     I = Inputs(cfg)
     p = I.p
     box = 1
@@ -321,9 +322,13 @@ def test_divb_correct(cfg, errlim):
     # both reduce the divergence; the GPU residual meets the reference criterion
     assert np.linalg.norm(dg) < np.linalg.norm(d0)
     assert np.linalg.norm(dg) <= 1.5 * np.linalg.norm(do) + 1e-6 * np.linalg.norm(d0)
-    corr_o = ob[0][box - 1] - b[0][box - 1]
-    corr_g = gb[0][box - 1] - b[0][box - 1]
-    assert rel_l2(corr_g, corr_o) < 0.2, (rel_l2(corr_g, corr_o), it_o, it_g.value)
+    # per component, the GPU's B is at least as close to the FP64 build's
+    # (within the stated slack) as the reference's FP32 solve is
+    import _divb_parity as D
+    b8, _ = D.divb_correct_r8(*I.dims(box), 7, pos, xs, errlim, *b)
+    for q in range(3):
+        eg, er = D.rel(gb[q][box - 1], b8[q][box - 1]), D.rel(ob[q][box - 1], b8[q][box - 1])
+        assert eg <= D.SLACK * er + D.FLOOR, (q, eg, er, it_o, it_g.value)
     assert abs(it_g.value - it_o) <= max(3, 0.25 * it_o), (it_g.value, it_o)
 
 
