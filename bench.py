@@ -270,6 +270,8 @@ def run_ours(args):
     }
     if not args.no_batched:
         line["batched"] = run_batched(args, local)
+    if not args.no_adjoint:
+        line["adjoint"] = run_adjoint(local)
     if not args.no_cpu and ws == 1:
         line["cpu_baseline"] = cpu_baseline()
     return line
@@ -335,6 +337,75 @@ def run_batched(args, device, members=16):
             "plain": {"value": vp, "unit": "cell-updates/s", "ms_per_step": ms_p / n_p, "steps": n_p,
                       "mode": "members one after another, kernels launched from the host loop"},
             "graph_over_plain": vg / vp, "member_graphs_over_plain": vm / vp, "streams_over_plain": vc / vp}
+
+
+ADJOINT_WORKLOAD = ("adjoint of 50 main steps on 3 nested boxes of 97x97x49 (2x refinement, sub-cycled, FP32 state, "
+                    "FP64 CG reductions, div B every 10 steps), checkpointed every 10 steps; misfit of B and density "
+                    "at 200 samples along a seeded straight line, gradient w.r.t. the 8 upstream wind-face parameters "
+                    "and the initial state")
+
+
+def run_adjoint(device, nsteps=50, every=10, nsamp=200):
+    """BASELINE config 3: the adjoint of 50 main steps of 3 nested 97x97x49
+    boxes, checkpointed every 10 steps.  Times (CUDA events on the model's
+    stream): the plain forward (the engine's step, graph-replayed), the
+    adjoint's forward (host-launched, with checkpoints and the misfit), and
+    the backward (each checkpoint interval re-run with snapshots, then every
+    kernel reversed).  adjoint_over_forward = backward / plain forward, per
+    main step."""
+    import torch
+    from g3m3_gb300.adjoint import MisfitRun, line_samples, wind_of
+    from g3m3_gb300.api import Context, Model
+    from g3m3_gb300.state import make_config
+    st = make_config("nested", limit=48, n_grids=3)
+    p = st.params
+    ctx = Context(device)
+    m = Model(ctx, st)
+    m.autotune()
+    stream = torch.cuda.ExternalStream(m.stream)
+
+    def ev_time(fn):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    # the plain forward: the same 50 main steps from the same state, graph-replayed
+    m.init_steps()
+    m.run(3, graph=True)                       # warm-up (graph captures)
+    m.upload(st)
+    m.init_steps()
+    cu0 = m.times()[2]
+    fwd_ms = ev_time(lambda: m.run(nsteps, graph=True))
+    cu = m.times()[2] - cu0
+    samples = line_samples(st, nsteps, n=nsamp)
+    run = MisfitRun(m, st, nsteps, samples, checkpoint_every=every)
+    w = wind_of(p)
+    run.loss(w)                                 # warm-up: records the schedule, allocates
+    run.adj.backward(state=False)
+    loss_box = {}
+    afwd_ms = ev_time(lambda: loss_box.setdefault("loss", run.loss(w)))
+    grads = {}
+    bwd_ms = ev_time(lambda: grads.update(run.adj.backward(state=False)))
+    tape = run.adj.tape_bytes()
+    run.adj.close()
+    m.close()
+    ctx.close()
+    return {"workload": ADJOINT_WORKLOAD, "boxes": p.n_grids, "box": [p.nx, p.ny, p.nz], "main_steps": nsteps,
+            "checkpoint_every": every, "samples": nsamp, "cell_updates": cu,
+            "forward_ms_per_step": fwd_ms / nsteps,
+            "adjoint_forward_ms_per_step": afwd_ms / nsteps,
+            "backward_ms_per_step": bwd_ms / nsteps,
+            "adjoint_over_forward": bwd_ms / fwd_ms,
+            "gradient_over_forward": (afwd_ms + bwd_ms) / fwd_ms,
+            "loss": loss_box["loss"], "grad_wind": [float(x) for x in grads["params"]],
+            "tape_bytes": tape,
+            "note": "forward: the engine's graph-replayed main steps; backward: per checkpoint interval the steps "
+                    "re-run with snapshots, then the reverse kernels"}
 
 
 KERNELS = {  # id: (name, launches per box-step)
@@ -489,6 +560,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the 16-member ensemble leg")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg (BASELINE config 3)")
+    ap.add_argument("--adjoint-only", action="store_true", help="run only the adjoint leg and print its block")
     ap.add_argument("--profile", action="store_true",
                     help="profiling case for ncu: one 121x121x61 box, warmup+steps main steps, host-loop launches")
     ap.add_argument("--profile-boxes", type=int, default=1,
@@ -496,6 +569,9 @@ def main():
     args = ap.parse_args()
     if args.profile:
         return run_profile(args)
+    if args.adjoint_only:
+        print(json.dumps({"adjoint": run_adjoint(0)}), flush=True)
+        return None
     line = run_reference(args) if args.impl == "reference" else run_ours(args)
     if line is not None:
         print(json.dumps(line), flush=True)

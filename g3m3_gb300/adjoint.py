@@ -100,6 +100,73 @@ class Adjoint:
             pass
 
 
+def sample_state(p, cur, xyz):
+    """(n, 4) trilinear values of bx, by, bz and the total density
+    qrho + hrho + orho at xyz (n, 3) [planet radii] in the smallest box
+    whose open extent holds the point (the library's misfit samples,
+    cft_findgrid.f90:70-126, cft_trilin_interp.f90:34-54); NaN where no
+    box holds it.  cur: (34, n_grids, nz, ny, nx) on the host."""
+    out = np.full((len(xyz), 4), np.nan)
+    for n, X in enumerate(np.asarray(xyz, np.float64)):
+        v = X / p.re_equiv
+        box = 0
+        for b in range(1, p.n_grids + 1):
+            mn = np.array([p.grd_xmin[b - 1], p.grd_ymin[b - 1], p.grd_zmin[b - 1]])
+            mx = np.array([p.grd_xmax[b - 1], p.grd_ymax[b - 1], p.grd_zmax[b - 1]])
+            if (v > mn).all() and (v < mx).all():
+                box = b
+                break
+        if box == 0:
+            continue
+        mn = np.array([p.grd_xmin[box - 1], p.grd_ymin[box - 1], p.grd_zmin[box - 1]])
+        sp = p.xspac[box - 1]
+        g = 1 + ((v - mn) / sp).astype(int)
+        if (g < 1).any() or g[0] >= p.nx or g[1] >= p.ny or g[2] >= p.nz:
+            continue
+        c0 = (mn + (g - 1) * sp) * p.re_equiv
+        w = (X - c0) / (sp * p.re_equiv)
+        i, j, k = g - 1
+        val = np.zeros(4)
+        for dk in (0, 1):
+            for dj in (0, 1):
+                for di in (0, 1):
+                    wt = (w[0] if di else 1 - w[0]) * (w[1] if dj else 1 - w[1]) * (w[2] if dk else 1 - w[2])
+                    c = (box - 1, k + dk, j + dj, i + di)
+                    for q in range(3):
+                        val[q] += wt * cur[31 + q][c]
+                    val[3] += wt * (cur[0][c] + cur[10][c] + cur[20][c])
+        out[n] = val
+    return out
+
+
+def line_samples(state, nsteps, n=200, seed=20261205, scale=0.1):
+    """A virtual spacecraft on a straight line: n samples through the
+    outermost box (x from 3 % to 97 % of its extent, y and z drawn from
+    the seed between 15 and 30 %, beside the planet), spread evenly over
+    the N main steps; targets are the initial state's values there times
+    (1 + scale N(0,1)), drawn from the seed."""
+    p = state.params
+    rng = np.random.default_rng(seed)
+    ng = p.n_grids
+    lo = np.array([p.grd_xmin[ng - 1], p.grd_ymin[ng - 1], p.grd_zmin[ng - 1]]) * p.re_equiv
+    hi = np.array([p.grd_xmax[ng - 1], p.grd_ymax[ng - 1], p.grd_zmax[ng - 1]]) * p.re_equiv
+    span = hi - lo
+    a = lo + span * np.array([0.03, 0.15 + 0.15 * rng.random(), 0.15 + 0.15 * rng.random()])
+    b = lo + span * np.array([0.97, 0.15 + 0.15 * rng.random(), 0.15 + 0.15 * rng.random()])
+    t = np.linspace(0.0, 1.0, n)
+    xyz = (a[None, :] + t[:, None] * (b - a)[None, :]).astype(np.float32)
+    step = (1 + (np.arange(n) * nsteps) // n).astype(np.int32)
+    v0 = sample_state(p, state.cur.astype(np.float64), xyz)
+    v0[np.isnan(v0)] = 0.0
+    target = (v0 * (1.0 + scale * rng.standard_normal(v0.shape))).astype(np.float32)
+    return xyz, step, target
+
+
+def wind_of(params):
+    """The eight wind-face parameters of a parameter block."""
+    return np.array([getattr(params, k) for k in WIND], np.float64)
+
+
 def wind_scales(setup):
     """Constants of the upstream conversion for a state.Setup: (1/rho_equiv *
     rmassq, 1/v_equiv, spress per unit srho, 1/b_equiv)."""

@@ -63,17 +63,24 @@ def test_wind_gradient_against_fp64_differences(cfg, nsteps, every, divb):
     assert err <= GRAD_TOL, (err, ga, fd)
 
 
-def test_state_gradient_directional():
-    ctx, st, samples, run = _run("tiny3", 3, 1, divb_every=0)
+@pytest.mark.parametrize("divb", [0, 2])
+def test_state_gradient_directional(divb):
+    """<dL/dstate, delta> for a random delta on all 34 fields against FP64
+    central differences along delta.  The misfit has kinks (the limiters'
+    max/min, the guards' floors and replacements): a step of 1e-4 crosses
+    some of them and biases the difference by up to 1 %, so h = 1e-7 of each
+    field's mean magnitude, well inside FP64's precision."""
+    over = dict(divb_every=divb, divb_errlim=1e-6) if divb else dict(divb_every=0)
+    ctx, st, samples, run = _run("tiny3", 4 if divb else 3, 2 if divb else 1, **over)
     w = R.wind_of(st)
     run.loss(w)
     sch = run.schedule
     grads = run.adj.backward()
     ctx.close()
-    rng = np.random.default_rng(11)
-    scale = np.abs(st.cur).reshape(34, -1).mean(axis=1)
+    rng = np.random.default_rng(5)
+    scale = np.abs(st.cur).reshape(34, -1).mean(axis=1) + 1e-3
     delta = np.stack([scale[q] * rng.standard_normal(st.cur.shape[1:]) for q in range(34)])
-    h = 1e-4
+    h = 1e-7
     fd = (R.oracle_loss(st, w, sch, samples, delta=h * delta) - R.oracle_loss(st, w, sch, samples,
                                                                                delta=-h * delta)) / (2 * h)
     ad = float((grads["state"].astype(np.float64) * delta).sum())
@@ -89,3 +96,32 @@ def test_checkpoint_interval_does_not_change_the_gradient():
         out.append(run.adj.backward()["params"])
         ctx.close()
     assert np.allclose(out[0], out[1], rtol=1e-5, atol=1e-9 * np.abs(out[0]).max()), out
+
+
+def test_torch_function_upstream_gradient():
+    """loss = WindMisfit(upstream_wind(u)); u.grad from torch's chain rule
+    through the CUDA adjoint equals J^T dL/dwind of the conversion."""
+    import torch
+    from g3m3_gb300.adjoint import WindMisfit, upstream_wind, wind_scales
+    from g3m3_gb300.state import Setup, CONFIGS
+    ctx, st, samples, run = _run("tiny3", 3, 3, divb_every=0)
+    setup = Setup(**CONFIGS["tiny3"])
+    w = setup.wind
+    u = torch.tensor([w.n_cm3, w.speed_kms, 0.0, 0.0, 0.0, w.b_nT * np.sin(w.clock_angle),
+                      w.b_nT * np.cos(w.clock_angle)], dtype=torch.float64, requires_grad=True)
+    wind = upstream_wind(u, setup)
+    assert np.allclose(wind.detach().numpy(), R.wind_of(st), rtol=1e-6, atol=1e-9)
+    loss = WindMisfit().apply(wind, run)
+    loss.backward()
+    gw = run.adj.backward(state=False)["params"]
+    ctx.close()
+    kr, kv, kp, kb = wind_scales(setup)
+    uu = u.detach().numpy()
+    J = np.zeros((8, 7))
+    J[0, 0] = kr
+    J[1, 0], J[1, 1] = kr * uu[1] * kv, kr * uu[0] * kv
+    J[2, 0], J[2, 2] = kr * uu[2] * kv, kr * uu[0] * kv
+    J[3, 0], J[3, 3] = kr * uu[3] * kv, kr * uu[0] * kv
+    J[4, 0] = kr * kp
+    J[5, 4] = J[6, 5] = J[7, 6] = kb
+    assert np.allclose(u.grad.numpy(), J.T @ gw, rtol=1e-6, atol=1e-12 * np.abs(J.T @ gw).max())
