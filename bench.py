@@ -392,6 +392,7 @@ def run_adjoint(device, nsteps=50, every=10, nsamp=200):
     grads = {}
     bwd_ms = ev_time(lambda: grads.update(run.adj.backward(state=False)))
     tape = run.adj.tape_bytes()
+    phases = run.adj.phases()
     run.adj.close()
     m.close()
     ctx.close()
@@ -404,6 +405,8 @@ def run_adjoint(device, nsteps=50, every=10, nsamp=200):
             "gradient_over_forward": (afwd_ms + bwd_ms) / fwd_ms,
             "loss": loss_box["loss"], "grad_wind": [float(x) for x in grads["params"]],
             "tape_bytes": tape,
+            "backward_phases_s": {"rerun_with_snapshots": phases[0], "reverse_kernels": phases[1],
+                                  "divb_reverse": phases[2]},
             "note": "forward: the engine's graph-replayed main steps; backward: per checkpoint interval the steps "
                     "re-run with snapshots, then the reverse kernels"}
 

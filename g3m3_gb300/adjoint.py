@@ -26,13 +26,10 @@ import numpy as np
 
 from .api import Model, addr
 from .params import NFIELDS
+from .state import EV, M_PROT, MU0
 
 WIND = ("srho", "spx", "spy", "spz", "spress", "sbx_wind", "sby_wind", "sbz_wind")
 
-# physical constants of the unit conversions (3d_main.f90:907-943)
-MU0 = 4.0e-7 * math.pi
-M_PROT = 1.6726e-27
-EV = 1.6022e-19
 
 
 class Adjoint:
@@ -84,6 +81,13 @@ class Adjoint:
         if rc not in (0, 3):   # 3: an adjoint div B solve hit its iteration cap (a warning)
             self.ctx.check(rc)
         return dict(params=gp, state=gs, wrk_epres=gw, noconv=rc == 3)
+
+    def phases(self):
+        """Seconds of the last backward: re-run with snapshots, reverse
+        kernels, reversed div B passes."""
+        out = (ctypes.c_double * 3)()
+        self.ctx.check(self.L.g3m3_adjoint_phases(self.h, out))
+        return list(out)
 
     def tape_bytes(self):
         return int(self.L.g3m3_adjoint_tape_bytes(self.h))
@@ -139,20 +143,20 @@ def sample_state(p, cur, xyz):
     return out
 
 
-def line_samples(state, nsteps, n=200, seed=20261205, scale=0.1):
+def line_samples(state, nsteps, n=200, seed=20261205, scale=0.1, x_end=0.4):
     """A virtual spacecraft on a straight line: n samples through the
-    outermost box (x from 3 % to 97 % of its extent, y and z drawn from
-    the seed between 15 and 30 %, beside the planet), spread evenly over
-    the N main steps; targets are the initial state's values there times
-    (1 + scale N(0,1)), drawn from the seed."""
+    outermost box, from 2 % of its x extent (next to the inflow face) to
+    x_end, y and z drawn from the seed between 15 and 30 % (beside the
+    planet), spread evenly over the N main steps; targets are the initial
+    state's values there times (1 + scale N(0,1)), drawn from the seed."""
     p = state.params
     rng = np.random.default_rng(seed)
     ng = p.n_grids
     lo = np.array([p.grd_xmin[ng - 1], p.grd_ymin[ng - 1], p.grd_zmin[ng - 1]]) * p.re_equiv
     hi = np.array([p.grd_xmax[ng - 1], p.grd_ymax[ng - 1], p.grd_zmax[ng - 1]]) * p.re_equiv
     span = hi - lo
-    a = lo + span * np.array([0.03, 0.15 + 0.15 * rng.random(), 0.15 + 0.15 * rng.random()])
-    b = lo + span * np.array([0.97, 0.15 + 0.15 * rng.random(), 0.15 + 0.15 * rng.random()])
+    a = lo + span * np.array([0.02, 0.15 + 0.15 * rng.random(), 0.15 + 0.15 * rng.random()])
+    b = lo + span * np.array([x_end, 0.15 + 0.15 * rng.random(), 0.15 + 0.15 * rng.random()])
     t = np.linspace(0.0, 1.0, n)
     xyz = (a[None, :] + t[:, None] * (b - a)[None, :]).astype(np.float32)
     step = (1 + (np.arange(n) * nsteps) // n).astype(np.int32)
@@ -170,7 +174,7 @@ def wind_of(params):
 def wind_scales(setup):
     """Constants of the upstream conversion for a state.Setup: (1/rho_equiv *
     rmassq, 1/v_equiv, spress per unit srho, 1/b_equiv)."""
-    gamma = 5.0 / 3.0
+    gamma = 1.6666   # the value state.py (3d_main.f90's gamma) uses
     b_equiv = setup.v_equiv * 1.0e3 * math.sqrt(MU0 * setup.rho_equiv * 1.0e6 * M_PROT) * 1.0e9
     cs_wind = math.sqrt(gamma * setup.wind.t_ev * EV / M_PROT) / 1.0e3 / setup.v_equiv
     return setup.rmassq / setup.rho_equiv, 1.0 / setup.v_equiv, (cs_wind ** 2 / gamma) / (gamma - 1.0), 1.0 / b_equiv

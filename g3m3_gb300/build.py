@@ -4,6 +4,7 @@ Every translation unit is compiled in parallel with nvcc for sm_103a only,
 with IEEE division and square root and no multiply-add contraction
 (-fmad=false): the kernels are written to reproduce the reference's FP32
 operation order bit for bit, and bandwidth, not arithmetic, bounds them.
+The reverse-mode kernels are the exception (FAST_MATH_FILES).
 """
 from __future__ import annotations
 
@@ -26,6 +27,19 @@ FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-pr
          # either: gcc contracts a*b+c into fma by default on aarch64
          "-Xcompiler", "-ffp-contract=off",
          "-I", os.path.join(HERE, "..", "include")]
+
+
+# The reverse-mode kernels (k_adj.cu) compute gradients, which no bitwise
+# comparison constrains: they build with contraction and the fast division
+# and square root.
+FAST_MATH_FILES = {"k_adj.cu"}
+FAST = {"-fmad=false": "-fmad=true", "-prec-div=true": "-prec-div=false", "-prec-sqrt=true": "-prec-sqrt=false"}
+
+
+def flags_for(src):
+    if os.path.basename(src) in FAST_MATH_FILES:
+        return [FAST.get(f, f) for f in FLAGS]
+    return FLAGS
 
 
 def nvcc():
@@ -57,7 +71,7 @@ def build(verbose: bool = False, extra=()) -> str:
         obj = os.path.join(BUILD_DIR, os.path.basename(src)[:-3] + ".o")
         objs.append(obj)
         if _stale(obj, [src] + headers + [__file__]):
-            jobs.append([nvcc(), *ARCH, *FLAGS, *extra, "-c", src, "-o", obj])
+            jobs.append([nvcc(), *ARCH, *flags_for(src), *extra, "-c", src, "-o", obj])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -19,6 +19,7 @@
 // state through set_speed_agrd's maxima is not differentiated); the div B
 // solves are differentiated as exact linear solves, so the gradient is that
 // of the converged projection.
+#include <chrono>
 #include <cstring>
 #include <vector>
 
@@ -189,6 +190,10 @@ struct g3m3_adjoint {
   CgState* host_cgst = nullptr;        // pinned
   double* d_aparam = nullptr;          // [8]
   Tape tape;
+  double phase_s[3] = {};              // last backward: re-run with snapshots, reverse kernels, div B reverse
+  bool prof = false;                   // GPU time per stage of the box-step reverses
+  cudaEvent_t ev[17] = {};
+  double stage_ms[16] = {};
   float* mem = nullptr;
   int64_t cell_updates = 0;
 };
@@ -468,6 +473,11 @@ void tab_of(float* base, size_t n3, float* t[G3M3_NFIELDS]) {
   for (int q = 0; q < G3M3_NFIELDS; q++) t[q] = base + (size_t)q * n3;
 }
 
+// GPU-time marks between the stages of a box-step's reverse (when profiling)
+void mark(g3m3_adjoint* A, int k) {
+  if (A->prof) cudaEventRecord(A->ev[k], A->m->stream);
+}
+
 // one recorded box-step in reverse (the engine's enqueue_box_step read
 // backwards; aC is the adjoint of cur, aW of wrk, aO of old = the start state)
 void rev_box(g3m3_adjoint* A, const BoxRec& R) {
@@ -482,6 +492,7 @@ void rev_box(g3m3_adjoint* A, const BoxRec& R) {
   // the adjoints after the box-step: cur's (aC); wrk's, of which only the
   // electron pressure is read later; old's (the start state as the finer
   // box's flanks read it after this step)
+  mark(A, 0);
   cudaMemsetAsync(A->aW, 0, (size_t)G3M3_NFIELDS * n3 * sizeof(float), s);
   {
     const float* we = A->a_we + (size_t)(b - 1) * n3;
@@ -497,7 +508,9 @@ void rev_box(g3m3_adjoint* A, const BoxRec& R) {
   tab_of(R.snap[TP_CORR_GUARD], n3, c1);
   tab_of(R.snap[TP_LAP_GUARD], n3, l1);
   // flux correction: guards, boundaries, fcsmooth of (wrk, old)
+  mark(A, 1);
   rev_guard(A, R.snap[TP_FCS_BNDRY], aC, b, true);
+  mark(A, 2);
   rev_boundary(A, R.snap[TP_FCS_BNDRY], aC, b, R.t1c, true);
   {
     AdjFcsArgs f{};
@@ -510,10 +523,13 @@ void rev_box(g3m3_adjoint* A, const BoxRec& R) {
       f.chi[q] = q >= G3M3_F_BX ? m->p.diferg : m->p.difrho;
     }
     f.p1 = A->p1; f.a_p1 = A->a_p1; f.nf = G3M3_NFIELDS; f.d = m->d;
+    mark(A, 3);
     launch_adj_fcs(f, s);
   }
   // Lapidus: guards, boundaries, the smoothing of the corrector's state
+  mark(A, 4);
   rev_guard(A, R.snap[TP_LAP_BNDRY], aW, b, true);
+  mark(A, 5);
   rev_boundary(A, R.snap[TP_LAP_BNDRY], aW, b, R.t1c, true);
   for (int sp = 0; sp < 3; sp++) {
     AdjLapArgs l{};
@@ -559,26 +575,45 @@ void rev_box(g3m3_adjoint* A, const BoxRec& R) {
     }
     for (int q = 0; q < 3; q++) v.a_v[q] = sc(A, SC_VT + q);
     v.d = m->d;
+    mark(A, 6);
     launch_adj_vtot(v, s);
   }
   // corrector: guards; boundaries (its flanks go to wrk, which Lapidus
   // overwrites before any read, so only bndry_inner / bndry_outer on cur
   // are reversed); the pushes from (wrk, old); the fields of wrk
+  mark(A, 7);
   rev_guard(A, R.snap[TP_CORR_BNDRY], aC, b, true);
+  mark(A, 8);
   rev_boundary(A, R.snap[TP_CORR_BNDRY], aC, b, R.t1c, false);
+  mark(A, 9);
   rev_push(A, w1, s0, aC, aW, aO, b, R.dt, true);
+  mark(A, 10);
   rev_fields(A, w1, aW, b);
   // predictor: guards, boundaries, the pushes from (old, old), the fields of old
+  mark(A, 11);
   rev_guard(A, R.snap[TP_PRED_BNDRY], aW, b, true);
+  mark(A, 12);
   rev_boundary(A, R.snap[TP_PRED_BNDRY], aW, b, R.t1p, true);
+  mark(A, 13);
   rev_push(A, s0, s0, aW, aO, aO, b, R.dt2, false);
+  mark(A, 14);
   rev_fields(A, s0, aO, b);
   // before the box-step: cur held the start state; wrk's epres the value
   // the predictor's push_elec read
+  mark(A, 15);
   launch_copy_fields_out(aC, A->aO, G3M3_NFIELDS, n3, s);
   const float* we = aW[G3M3_F_EPRES];
   float* dst = A->a_we + (size_t)(b - 1) * n3;
   launch_copy_fields_out(&dst, we, 1, n3, s);
+  mark(A, 16);
+  if (A->prof) {
+    cudaEventSynchronize(A->ev[16]);
+    for (int q = 0; q < 16; q++) {
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, A->ev[q], A->ev[q + 1]);
+      A->stage_ms[q] += ms;
+    }
+  }
 }
 
 void loss_args(g3m3_adjoint* A, LossArgs& L, int first, int count) {
@@ -746,6 +781,8 @@ int g3m3_adjoint_destroy(g3m3_adjoint* A) {
   cudaFree(A->d_resid);
   if (A->host_cgst) cudaFreeHost(A->host_cgst);
   if (A->h_loss) cudaFreeHost(A->h_loss);
+  for (int q = 0; q < 17; q++)
+    if (A->ev[q]) cudaEventDestroy(A->ev[q]);
   delete A;
   return G3M3_OK;
 }
@@ -824,6 +861,15 @@ int g3m3_adjoint_backward(g3m3_adjoint* A, double* grad_params, float* grad_stat
   G3M3_CUDA(m->ctx, cudaMemsetAsync(A->d_aparam, 0, 8 * sizeof(double), s));
   int rc = G3M3_OK;
   int worst = G3M3_OK;
+  for (double& t : A->phase_s) t = 0.0;
+  using clk = std::chrono::steady_clock;
+  auto lap = [&](clk::time_point& t0, int phase) {   // phase time, the stream drained
+    cudaStreamSynchronize(s);
+    const clk::time_point t1 = clk::now();
+    A->phase_s[phase] += std::chrono::duration<double>(t1 - t0).count();
+    t0 = t1;
+  };
+  clk::time_point t0 = clk::now();
   for (int seg = A->nseg - 1; seg >= 0 && !rc; seg--) {
     const int s0 = seg * A->every;
     const int s1 = s0 + A->every < A->nsteps ? s0 + A->every : A->nsteps;
@@ -833,6 +879,7 @@ int g3m3_adjoint_backward(g3m3_adjoint* A, double* grad_params, float* grad_stat
     rc = run_forced(A, s0, s1);
     m->tape = nullptr;
     if (rc) break;
+    lap(t0, 0);
     const Tape& T = A->tape;
     for (int st = s1 - 1; st >= s0 && !rc; st--) {
       const int k = st - s0;
@@ -860,9 +907,11 @@ int g3m3_adjoint_backward(g3m3_adjoint* A, double* grad_params, float* grad_stat
             break;
           }
           case Rec::DIVB: {
+            lap(t0, 1);
             const int st2 = rev_divb(A);
             if (st2 == G3M3_ERR_NOCONV) worst = st2;
             else rc = st2;
+            lap(t0, 2);
             break;
           }
         }
@@ -870,6 +919,7 @@ int g3m3_adjoint_backward(g3m3_adjoint* A, double* grad_params, float* grad_stat
         if (e != cudaSuccess) rc = cuda_check(m->ctx, e, "adjoint");
       }
     }
+    lap(t0, 1);
   }
   // leave the model at the end of the run, as the forward did
   if (!rc) rc = load_ckpt(A, A->nseg);
@@ -883,6 +933,23 @@ int g3m3_adjoint_backward(g3m3_adjoint* A, double* grad_params, float* grad_stat
     G3M3_CUDA(m->ctx, cudaMemcpyAsync(grad_wrk_epres, A->a_we, n4 * sizeof(float), cudaMemcpyDefault, s));
   G3M3_CUDA(m->ctx, cudaStreamSynchronize(s));
   return worst;
+}
+
+int g3m3_adjoint_profile(g3m3_adjoint* A, int on, double* stage_ms) {
+  if (!A) return G3M3_ERR_ARG;
+  if (stage_ms)
+    for (int q = 0; q < 16; q++) stage_ms[q] = A->stage_ms[q];
+  for (int q = 0; q < 16; q++) A->stage_ms[q] = 0.0;
+  if (on && !A->ev[0])
+    for (int q = 0; q < 17; q++) G3M3_CUDA(A->m->ctx, cudaEventCreate(&A->ev[q]));
+  A->prof = on != 0;
+  return G3M3_OK;
+}
+
+int g3m3_adjoint_phases(g3m3_adjoint* A, double* seconds) {
+  if (!A || !seconds) return G3M3_ERR_ARG;
+  for (int q = 0; q < 3; q++) seconds[q] = A->phase_s[q];
+  return G3M3_OK;
 }
 
 size_t g3m3_adjoint_tape_bytes(g3m3_adjoint* A) {

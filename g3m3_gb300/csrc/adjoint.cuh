@@ -108,6 +108,7 @@ struct AdjFcsArgs {              // flux correction of nf fields
   float* a_old[G3M3_NFIELDS];
   float chi[G3M3_NFIELDS];
   int nf;
+  int clear_px;                  // set by the launcher: k_adj_p1 clears a_px (the gather form)
   Dims d;
 };
 

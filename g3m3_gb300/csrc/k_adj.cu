@@ -39,6 +39,40 @@ __device__ __forceinline__ Cell3 cell3(const Dims& d) {
   return r;
 }
 
+// the cells of the one-deep outer shell: x faces, then y faces (x
+// interior), then z faces (x and y interior)
+__device__ bool shell1_cell(long t, const Dims& d, int& i, int& j, int& k) {
+  const long nyz = (long)d.ny * d.nz;
+  if (t < 2 * nyz) {
+    i = t < nyz ? 1 : d.nx;
+    const long r = t % nyz;
+    j = (int)(r % d.ny) + 1;
+    k = (int)(r / d.ny) + 1;
+    return true;
+  }
+  t -= 2 * nyz;
+  const int ix = d.nx - 2;
+  const long nxz = (long)ix * d.nz;
+  if (t < 2 * nxz) {
+    j = t < nxz ? 1 : d.ny;
+    const long r = t % nxz;
+    i = (int)(r % ix) + 2;
+    k = (int)(r / ix) + 1;
+    return true;
+  }
+  t -= 2 * nxz;
+  const int iy = d.ny - 2;
+  const long nxy = (long)ix * iy;
+  if (t < 2 * nxy) {
+    k = t < nxy ? 1 : d.nz;
+    const long r = t % nxy;
+    i = (int)(r % ix) + 2;
+    j = (int)(r / ix) + 2;
+    return true;
+  }
+  return false;
+}
+
 // offsets of the 7-point stencil in the order c, xp, xm, yp, ym, zp, zm
 struct Off7 {
   long o[7];
@@ -49,22 +83,16 @@ struct Off7 {
 };
 
 // ------------------------------------------------------------------ push_ion
-__global__ void __launch_bounds__(128) k_adj_push_ion(const __grid_constant__ AdjPushIonArgs a) {
+// 168 registers (three blocks of 128 per SM; a small spill) timed fastest
+// against the unbounded 255, 128 and 80; a form that sums the stencil
+// contributions of a tile in a shared-memory ring with shared atomics before
+// adding them to global memory was slower (289 against 226 us per launch on
+// a 97x97x49 box, both with IEEE division) and is not kept.
+__global__ void __launch_bounds__(128, 3) k_adj_push_ion(const __grid_constant__ AdjPushIonArgs a) {
   const Dims d = a.d;
   const Cell3 p = cell3(d);
-  if (!p.ok) return;
+  if (!p.ok || !p.interior) return;   // the boundary: k_adj_push_ion_shell
   const size_t c = p.c;
-  if (!p.interior) {
-    if (a.boundary_from_old) {
-#pragma unroll
-      for (int f = 0; f < 10; f++) {
-        const float g = a.a_out[f][c];
-        if (g != 0.0f) red(a.a_old[f] + c, g);
-        a.a_out[f][c] = 0.0f;
-      }
-    }
-    return;
-  }
   float ob[10];
   bool any = false;
 #pragma unroll
@@ -113,6 +141,20 @@ __global__ void __launch_bounds__(128) k_adj_push_ion(const __grid_constant__ Ad
       red(a.a_tv[s - 105] + c, v);
     }
   });
+}
+
+// the boundary cells of out: copies of old when the push wrote them
+__global__ void __launch_bounds__(256) k_adj_push_ion_shell(const __grid_constant__ AdjPushIonArgs a) {
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  int i, j, k;
+  if (!shell1_cell(t, a.d, i, j, k)) return;
+  const size_t c = a.d.at(i, j, k);
+#pragma unroll
+  for (int f = 0; f < 10; f++) {
+    const float g = a.a_out[f][c];
+    if (g != 0.0f) red(a.a_old[f] + c, g);
+    a.a_out[f][c] = 0.0f;
+  }
 }
 
 // ---------------------------------------------------- push_elec, push_bfld
@@ -463,6 +505,76 @@ __global__ void __launch_bounds__(256) k_adj_fcs(const __grid_constant__ AdjFcsA
   fcs_flux_adj<2>(a, f, i, j, k, k - 1, g);
 }
 
+// The same reverse as a gather, without atomics.  Along each axis the flux
+// at face m (2 <= m <= n-1; the reference clamps end faces onto these)
+// enters output cell m with -1, cell m+1 with +1 (m+1 <= n-1) and, for
+// m = 2, cell 2 once more with +1 (cell 2's lower face is clamped onto
+// face 2).  So a face's adjoint is a combination of the outputs' adjoints
+// around it, and a point's share of the faces that read it (faces m-2 ..
+// m+1) is gathered by the thread of that point.  The thread then holds the
+// whole adjoint of P1 at its cell (stored) and the flux and direct parts of
+// wrk's (added); k_adj_p1 finishes with P1's dependence on wrk and old.
+template <int AX>
+__device__ __forceinline__ void fcs_axis_gather(const AdjFcsArgs& a, int f, int i, int j, int k, float& accP,
+                                                float& accW) {
+  const Dims& d = a.d;
+  const int n = AX == 0 ? d.nx : (AX == 1 ? d.ny : d.nz);
+  const int p = AX == 0 ? i : (AX == 1 ? j : k);
+  auto at = [&](int t) { return AX == 0 ? d.at(t, j, k) : (AX == 1 ? d.at(i, t, k) : d.at(i, j, t)); };
+  const float* Apx = a.a_px[f];
+  // the pass of this axis runs for cells off the k faces (x, y) or for all
+  // cells of an interior k plane (z)
+  const bool pass = AX == 2 ? true : (k != 1 && k != d.nz);
+  if (!pass) return;
+  auto A = [&](int t) { return __ldg(Apx + at(t)); };
+  const size_t cells = d.cells();
+  const float* P = a.p1 + (size_t)f * cells;
+  const float* W = a.wrk[f];
+  const float par[1] = {a.chi[f]};
+  const int m_lo = p - 2 > 2 ? p - 2 : 2;
+  const int m_hi = p + 1 < n - 1 ? p + 1 : n - 1;
+  for (int m = m_lo; m <= m_hi; m++) {
+    float g = -A(m);
+    if (m + 1 <= n - 1) g += A(m + 1);
+    if (m == 2) g += A(2);
+    if (g == 0.0f) continue;
+    const int q = m + 1 > n - 1 ? n - 1 : m + 1;
+    const int idx[6] = {m - 1, m, q, q + 1, m, m + 1};
+    float in[6];
+    for (int t = 0; t < 4; t++) in[t] = __ldg(P + at(idx[t]));
+    in[4] = __ldg(W + at(idx[4]));
+    in[5] = __ldg(W + at(idx[5]));
+    adj::fcs_flux_cell<float>::adj(in, par, &g, [&](int s, float v) {
+      if (idx[s] != p) return;
+      if (s < 4) accP += v;
+      else accW += v;
+    });
+  }
+}
+
+__global__ void __launch_bounds__(256) k_adj_fcs_gather(const __grid_constant__ AdjFcsArgs a) {
+  const Dims d = a.d;
+  const Cell3 p = cell3(d);
+  const int zb = (d.nz + blockDim.z - 1) / blockDim.z;
+  const int f = blockIdx.z / zb;
+  if (f >= a.nf) return;
+  const int i = p.i, j = p.j;
+  const int k = (blockIdx.z % zb) * blockDim.z + threadIdx.z + 1;
+  if (i > d.nx || j > d.ny || k > d.nz) return;
+  const size_t c = d.at(i, j, k);
+  float accP = 0.0f, accW = 0.0f;
+  const float g = __ldg(a.a_px[f] + c);
+  if (k == 1 || k == d.nz || i == 1 || i == d.nx) accW += g;   // px = wrk there (x pass: t = wrk)
+  else accP += g;                                              // t = P1
+  // every point gathers along every axis: a boundary point is read by the
+  // faces next to it even where its own cell takes no flux
+  fcs_axis_gather<0>(a, f, i, j, k, accP, accW);
+  fcs_axis_gather<1>(a, f, i, j, k, accP, accW);
+  fcs_axis_gather<2>(a, f, i, j, k, accP, accW);
+  a.a_p1[(size_t)f * d.cells() + c] = accP;
+  if (accW != 0.0f) a.a_wrk[f][c] += accW;
+}
+
 // P1 = W + chi Lap7(O) in the interior, W on the boundary: gathered
 __global__ void __launch_bounds__(256) k_adj_p1(const __grid_constant__ AdjFcsArgs a) {
   const Dims d = a.d;
@@ -489,6 +601,7 @@ __global__ void __launch_bounds__(256) k_adj_p1(const __grid_constant__ AdjFcsAr
   if (inner(i, j, k - 1)) s += G[c - (size_t)d.nx * d.ny];
   if (inner(i, j, k)) s -= 6.0f * g;
   if (s != 0.0f) a.a_old[f][c] += a.chi[f] * s;
+  if (a.clear_px) a.a_px[f][c] = 0.0f;   // px was overwritten: its adjoint before is zero
 }
 
 // ---------------------------------------------------------------- guards
@@ -797,39 +910,6 @@ __device__ void outer_adj(OuterA& o, int i, int j, int k, float g) {
   }
 }
 
-__device__ bool shell1(long t, const Dims& d, int& i, int& j, int& k) {
-  // the cells of the one-deep outer shell: x faces, then y faces (x interior), then z faces
-  const long nyz = (long)d.ny * d.nz;
-  if (t < 2 * nyz) {
-    i = t < nyz ? 1 : d.nx;
-    const long r = t % nyz;
-    j = (int)(r % d.ny) + 1;
-    k = (int)(r / d.ny) + 1;
-    return true;
-  }
-  t -= 2 * nyz;
-  const int ix = d.nx - 2;
-  const long nxz = (long)ix * d.nz;
-  if (t < 2 * nxz) {
-    j = t < nxz ? 1 : d.ny;
-    const long r = t % nxz;
-    i = (int)(r % ix) + 2;
-    k = (int)(r / ix) + 1;
-    return true;
-  }
-  t -= 2 * nxz;
-  const int iy = d.ny - 2;
-  const long nxy = (long)ix * iy;
-  if (t < 2 * nxy) {
-    k = t < nxy ? 1 : d.nz;
-    const long r = t % nxy;
-    i = (int)(r % ix) + 2;
-    j = (int)(r / ix) + 2;
-    return true;
-  }
-  return false;
-}
-
 __global__ void __launch_bounds__(256) k_adj_outer(const __grid_constant__ AdjOuterArgs a) {
   const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const int f = blockIdx.y;
@@ -839,7 +919,7 @@ __global__ void __launch_bounds__(256) k_adj_outer(const __grid_constant__ AdjOu
   o.comp = f < 30 ? ((f % 10) >= 1 && (f % 10) <= 3 ? f % 10 : 0) : 0;
   for (int q = 0; q < 8; q++) o.gp[q] = 0.0;
   int i, j, k;
-  if (shell1(t, a.d, i, j, k)) {
+  if (shell1_cell(t, a.d, i, j, k)) {
     const size_t c = a.d.at(i, j, k);
     const float g = a.a[f][c];
     a.a[f][c] = 0.0f;   // every shell value was overwritten
@@ -1020,7 +1100,7 @@ __global__ void __launch_bounds__(256) k_adj_synced(const __grid_constant__ AdjS
   const int q = blockIdx.y;
   int is, js, ks;
   const Dims d = a.d;
-  if (!shell1(t, d, is, js, ks)) return;
+  if (!shell1_cell(t, d, is, js, ks)) return;
   const size_t c = d.at(is, js, ks);
   const float g = a.a_fine[q][c];
   a.a_fine[q][c] = 0.0f;
@@ -1214,6 +1294,10 @@ inline dim3 cells_grid(const Dims& d, const dim3& b) { return grid3(d, b); }
 }  // namespace
 
 void launch_adj_push_ion(const AdjPushIonArgs& a, cudaStream_t s) {
+  if (a.boundary_from_old) {
+    const long n = shell_count(a.d, 1);
+    k_adj_push_ion_shell<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
+  }
   const dim3 blk(32, 2, 2);
   k_adj_push_ion<<<cells_grid(a.d, blk), blk, 0, s>>>(a);
 }
@@ -1242,14 +1326,30 @@ void launch_adj_vtot(const AdjVtotArgs& a, cudaStream_t s) {
   k_adj_vtot<<<pw, 256, 0, s>>>(a);
 }
 
+// the scatter form (atomic reductions of every flux's contributions): the
+// direct statement, kept to check the gather form against
+void launch_adj_fcs_scatter(const AdjFcsArgs& a, cudaStream_t s) {
+  const dim3 blk(32, 4, 2);
+  const unsigned zb = (unsigned)((a.d.nz + blk.z - 1) / blk.z);
+  const dim3 grd((unsigned)((a.d.nx + blk.x - 1) / blk.x), (unsigned)((a.d.ny + blk.y - 1) / blk.y),
+                 zb * (unsigned)a.nf);
+  AdjFcsArgs b = a;
+  b.clear_px = 0;
+  k_fcs_p1<<<grd, blk, 0, s>>>(b);
+  k_adj_fcs<<<grd, blk, 0, s>>>(b);
+  k_adj_p1<<<grd, blk, 0, s>>>(b);
+}
+
 void launch_adj_fcs(const AdjFcsArgs& a, cudaStream_t s) {
   const dim3 blk(32, 4, 2);
   const unsigned zb = (unsigned)((a.d.nz + blk.z - 1) / blk.z);
   const dim3 grd((unsigned)((a.d.nx + blk.x - 1) / blk.x), (unsigned)((a.d.ny + blk.y - 1) / blk.y),
                  zb * (unsigned)a.nf);
   k_fcs_p1<<<grd, blk, 0, s>>>(a);
-  k_adj_fcs<<<grd, blk, 0, s>>>(a);
-  k_adj_p1<<<grd, blk, 0, s>>>(a);
+  AdjFcsArgs b = a;
+  b.clear_px = 1;
+  k_adj_fcs_gather<<<grd, blk, 0, s>>>(b);
+  k_adj_p1<<<grd, blk, 0, s>>>(b);
 }
 
 void launch_adj_guard(const AdjGuardArgs& a, cudaStream_t s) {

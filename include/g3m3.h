@@ -423,6 +423,17 @@ int g3m3_adjoint_schedule(g3m3_adjoint* a, double* out);
 int g3m3_adjoint_backward(g3m3_adjoint* a, double* grad_params,
     float* grad_state, float* grad_wrk_epres);
 size_t g3m3_adjoint_tape_bytes(g3m3_adjoint* a);
+/* Wall-clock seconds of the last backward's phases: [0] the re-run of the
+ * steps with snapshots, [1] the reverse kernels, [2] the reversed div B
+ * passes (their adjoint solves). */
+int g3m3_adjoint_phases(g3m3_adjoint* a, double* seconds);
+/* Per-stage GPU time of the box-step reverses (CUDA events between the
+ * stages; on = 1 turns it on for the next backward, which then waits for
+ * each box-step): stage_ms (16, may be null) receives the sums since the
+ * last call -- set-up, flux-correction guards, boundaries, fcsmooth,
+ * Lapidus guards, boundaries, Lapidus, corrector guards, boundaries,
+ * pushes, fields, predictor guards, boundaries, pushes, fields, hand-back. */
+int g3m3_adjoint_profile(g3m3_adjoint* a, int on, double* stage_ms);
 
 /* ---- a19: virtual spacecraft -- findgrid cft_findgrid.f90:4 and
  * trilin_interp cft_trilin_interp.f90:10, batched over n trajectory points:
