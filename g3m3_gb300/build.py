@@ -53,6 +53,23 @@ def sources():
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
 
 
+# Sources also built in the contracted flavour (FMA contraction, quotients
+# by shared denominators as reciprocal products), into g3m3::contracted.
+CONTRACTED_FILES = {"k_push_tiled.cu"}
+
+
+def units():
+    """(source, object, extra flags) of every translation unit."""
+    out = []
+    for src in sources():
+        base = os.path.basename(src)[:-3]
+        out.append((src, os.path.join(BUILD_DIR, base + ".o"), flags_for(src)))
+        if os.path.basename(src) in CONTRACTED_FILES:
+            fl = [FAST.get(f, f) if f == "-fmad=false" else f for f in FLAGS] + ["-DG3M3_CONTRACTED"]
+            out.append((src, os.path.join(BUILD_DIR, base + "_contracted.o"), fl))
+    return out
+
+
 def _stale(target, deps):
     if not os.path.exists(target):
         return True
@@ -67,11 +84,10 @@ def build(verbose: bool = False, extra=()) -> str:
     headers += [os.path.join(HERE, "..", "include", f) for f in os.listdir(os.path.join(HERE, "..", "include"))]
     jobs = []
     objs = []
-    for src in sources():
-        obj = os.path.join(BUILD_DIR, os.path.basename(src)[:-3] + ".o")
+    for src, obj, fl in units():
         objs.append(obj)
         if _stale(obj, [src] + headers + [__file__]):
-            jobs.append([nvcc(), *ARCH, *flags_for(src), *extra, "-c", src, "-o", obj])
+            jobs.append([nvcc(), *ARCH, *fl, *extra, "-c", src, "-o", obj])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -9,6 +9,9 @@ namespace g3m3 {
 
 cudaError_t prepare_fcsmooth();
 cudaError_t prepare_push_ion();
+namespace contracted {
+cudaError_t prepare_push_ion();
+}
 
 namespace {
 
@@ -58,6 +61,7 @@ cudaError_t prepare_smem(const void* func, int bytes) {
 cudaError_t prepare_device_kernels() {
   cudaError_t e = prepare_fcsmooth();
   if (e == cudaSuccess) e = prepare_push_ion();
+  if (e == cudaSuccess) e = contracted::prepare_push_ion();
   return e;
 }
 

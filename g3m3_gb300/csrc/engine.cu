@@ -201,6 +201,7 @@ void push_stage(g3m3_model* m, Getter out, Getter src, int b, int slot_dt, bool 
     a.rmass = masses[s]; a.grav = m->p.grav; a.re_equiv = m->p.re_equiv; a.reynolds = m->p.reynolds;
     a.delt = sref(m, slot_dt);
     a.boundary_from_old = out_is_cur ? 1 : 0;
+    a.contracted = m->contracted;
     launch_push_ion(a, m->aux[s]);
     m->launches_in_step += 1;
   }
@@ -1285,7 +1286,7 @@ int g3m3_model_time_kernel(g3m3_model* m, int kernel, int box, int reps, float* 
         a.g.dy = (p.grd_ymax[b - 1] - p.grd_ymin[b - 1]) / (float)(m->d.ny - 1);
         a.g.dz = (p.grd_zmax[b - 1] - p.grd_zmin[b - 1]) / (float)(m->d.nz - 1);
         a.rmass = p.rmassq; a.grav = p.grav; a.re_equiv = p.re_equiv; a.reynolds = p.reynolds;
-        a.delt = sref(m, slot); a.boundary_from_old = 0;
+        a.delt = sref(m, slot); a.boundary_from_old = 0; a.contracted = m->contracted;
         launch_push_ion(a, s);
         by = 160.0 * inner;     // 30 arrays read, 10 written per interior cell
         return 0;
@@ -1671,6 +1672,17 @@ int g3m3_model_fluxes(g3m3_model* m, float* out, int* nsteps) {
     }
   }
   if (nsteps) *nsteps = (int)n;
+  return G3M3_OK;
+}
+
+int g3m3_model_set_contracted(g3m3_model* m, int on) {
+  if (!m) return G3M3_ERR_ARG;
+  if (m->contracted != (on != 0)) {
+    for (auto& kv : m->graphs) cudaGraphExecDestroy(kv.second);   // graphs hold the other kernels
+    m->graphs.clear();
+    m->kernel_nodes.clear();
+    m->contracted = on != 0;
+  }
   return G3M3_OK;
 }
 

@@ -237,8 +237,14 @@ __global__ void __launch_bounds__(256) k_push_field(const __grid_constant__ Push
 }  // namespace
 
 void launch_push_ion_tiled(const PushIonArgs& a, cudaStream_t s);
+namespace contracted {
+void launch_push_ion_tiled(const PushIonArgs& a, cudaStream_t s);
+}
 
-void launch_push_ion(const PushIonArgs& a, cudaStream_t s) { launch_push_ion_tiled(a, s); }
+void launch_push_ion(const PushIonArgs& a, cudaStream_t s) {
+  if (a.contracted) contracted::launch_push_ion_tiled(a, s);
+  else launch_push_ion_tiled(a, s);
+}
 
 // The per-cell form (every neighbour through the L1 cache): the direct
 // statement of the stencil, kept for reference; the tiled kernel replaces it.

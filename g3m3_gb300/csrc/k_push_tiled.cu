@@ -14,7 +14,23 @@
 #include "kargs.cuh"
 #include "launch.cuh"
 
+// Built twice.  The default object keeps the reference's FP32 operation
+// order bit for bit (no contraction, quotients correctly rounded).  With
+// G3M3_CONTRACTED (and -fmad=true) the same kernel goes to the namespace
+// g3m3::contracted: products and sums contract to fused multiply-adds and a
+// quotient by a shared denominator is a product with its reciprocal
+// (within 1.5 ulp); the engine runs it when the model's contracted flavour
+// is on (g3m3_model_set_contracted).
+#ifdef G3M3_CONTRACTED
+#define QUOT(x_, d_, r_) ((x_) * (r_))
+#else
+#define QUOT(x_, d_, r_) div_by((x_), (d_), (r_))
+#endif
+
 namespace g3m3 {
+#ifdef G3M3_CONTRACTED
+namespace contracted {
+#endif
 
 namespace {
 
@@ -100,7 +116,7 @@ __device__ __forceinline__ void push_cell(const float* __restrict__ Plm, const f
   const float aqpz = old3 - delt * fluxdiv(3);
   float abx = C0(10), aby = C0(11), abz = C0(12);
   float bmag = bt;
-  const float weight = amax1(1.0f, div_by(bmag, bmax, r_bmax));
+  const float weight = amax1(1.0f, QUOT(bmag, bmax, r_bmax));
   const float skin_depth = rey / weight;
   const float tcx = (tvy * abz - tvz * aby);
   const float tcy = -(tvx * abz - tvz * abx);
@@ -119,7 +135,7 @@ __device__ __forceinline__ void push_cell(const float* __restrict__ Plm, const f
   const float dvy = (qcy - tcy) * skin_depth;
   const float dvz = (qcz - tcz) * skin_depth;
   const float rho_c = C0(0);
-  const float qden = div_by(rho_c, a.rmass, r_rmass);
+  const float qden = QUOT(rho_c, a.rmass, r_rmass);
   const float npx = aqpx + delt * (qden * (dex + dvx) - gpx);
   const float npy = aqpy + delt * (qden * (dey + dvy) - gpy);
   const float npz = aqpz + delt * (qden * (dez + dvz) - gpz);
@@ -130,29 +146,29 @@ __device__ __forceinline__ void push_cell(const float* __restrict__ Plm, const f
   const float rr = a.re_equiv * radius;
   const float g = delt * rho_c * a.grav / (rr * rr);
   const float r_radius = 1.0f / radius;
-  const float o_px = npx - div_by(g * ax, radius, r_radius);
-  const float o_py = npy - div_by(g * ay, radius, r_radius);
-  const float o_pz = npz - div_by(g * az, radius, r_radius);
+  const float o_px = npx - QUOT(g * ax, radius, r_radius);
+  const float o_py = npy - QUOT(g * ay, radius, r_radius);
+  const float o_pz = npz - QUOT(g * az, radius, r_radius);
 
   const float wx = C0(4), wy = C0(5), wz = C0(6), wxy = C0(7), wxz = C0(8), wyz = C0(9);
   const float t2 = 2.0f * delt;
   const float px_ = old4 - delt * fluxdiv(4) - DV(t2 * wx * (XP(VX) - XM(VX)), dxt, rdx);
   const float py_ = old5 - delt * fluxdiv(5) - DV(t2 * wy * (YP(VY) - YM(VY)), dyt, rdy);
   const float pz_ = old6 - delt * fluxdiv(6) - DV(t2 * wz * (ZP(VZ) - ZM(VZ)), dzt, rdz);
-  abx = div_by(6.0f * abx + XP(10) + XM(10) + YP(10) + YM(10) + ZP(10) + ZM(10), 12.0f, r12);
-  aby = div_by(6.0f * aby + XP(11) + XM(11) + YP(11) + YM(11) + ZP(11) + ZM(11), 12.0f, r12);
-  abz = div_by(6.0f * abz + XP(12) + XM(12) + YP(12) + YM(12) + ZP(12) + ZM(12), 12.0f, r12);
+  abx = QUOT(6.0f * abx + XP(10) + XM(10) + YP(10) + YM(10) + ZP(10) + ZM(10), 12.0f, r12);
+  aby = QUOT(6.0f * aby + XP(11) + XM(11) + YP(11) + YM(11) + ZP(11) + ZM(11), 12.0f, r12);
+  abz = QUOT(6.0f * abz + XP(12) + XM(12) + YP(12) + YM(12) + ZP(12) + ZM(12), 12.0f, r12);
   bmag = sqrtf(abx * abx + aby * aby + abz * abz);
   float skin = rey;
   if (bmag > bmax) skin = rey * (bmax / bmag);
-  const float gy2 = div_by(t2 * skin, a.rmass, r_rmass);
+  const float gy2 = QUOT(t2 * skin, a.rmass, r_rmass);
   const float o_xx = px_ - DV(t2 * wxy * (YP(VX) - YM(VX)), dyt, rdy) - DV(t2 * wxz * (ZP(VX) - ZM(VX)), dzt, rdz)
                      + gy2 * (wxy * abz - wxz * aby);
   const float o_yy = py_ - DV(t2 * wxy * (XP(VY) - XM(VY)), dxt, rdx) - DV(t2 * wyz * (ZP(VY) - ZM(VY)), dzt, rdz)
                      + gy2 * (wyz * abx - wxy * abz);
   const float o_zz = pz_ - DV(t2 * wxz * (XP(VZ) - XM(VZ)), dxt, rdx) - DV(t2 * wyz * (YP(VZ) - YM(VZ)), dyt, rdy)
                      + gy2 * (wxz * aby - wyz * abx);
-  const float gy1 = div_by(delt * skin, a.rmass, r_rmass);
+  const float gy1 = QUOT(delt * skin, a.rmass, r_rmass);
   const float o_xy = old7 - delt * fluxdiv(7)
                      - delt * wxy * (DV(XP(VX) - XM(VX), dxt, rdx) + DV(YP(VY) - YM(VY), dyt, rdy))
                      - DV(delt * wy * (YP(VX) - YM(VX)), dyt, rdy)
@@ -209,9 +225,9 @@ __global__ void __launch_bounds__(TX* TY, 3) k_push_ion_tiled(const __grid_const
         for (int f = 0; f < NLOAD; f++) v[f] = __ldg(src[f] + c);
         const float r = amax1(v[0], 1.e-6f);
         const float rr = 1.0f / r;
-        S(sm, slot, VX, ly, lx) = div_by(v[1], r, rr);
-        S(sm, slot, VY, ly, lx) = div_by(v[2], r, rr);
-        S(sm, slot, VZ, ly, lx) = div_by(v[3], r, rr);
+        S(sm, slot, VX, ly, lx) = QUOT(v[1], r, rr);
+        S(sm, slot, VY, ly, lx) = QUOT(v[2], r, rr);
+        S(sm, slot, VZ, ly, lx) = QUOT(v[3], r, rr);
       } else {
 #pragma unroll
         for (int f = 0; f < NLOAD; f++) v[f] = 0.0f;
@@ -287,4 +303,7 @@ void launch_push_ion_tiled(const PushIonArgs& a, cudaStream_t s) {
   }
 }
 
+#ifdef G3M3_CONTRACTED
+}  // namespace contracted
+#endif
 }  // namespace g3m3

@@ -29,6 +29,7 @@ struct PushIonArgs {
   float rmass, grav, re_equiv, reynolds;
   ScalarRef delt;
   int boundary_from_old;   // also set out = old on the boundary cells
+  int contracted;          // run the contracted flavour (g3m3::contracted)
 };
 
 struct PushFieldArgs {     // push_elec and push_bfld in one pass

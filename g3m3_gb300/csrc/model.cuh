@@ -84,6 +84,7 @@ struct g3m3_model {
   std::vector<int> h_ij[3];          // host copies of the inner-boundary tables (fluid files)
   std::vector<float> h_parm[3];
   int fcs_variant = 0;               // fcsmooth tile shape (g3m3_model_autotune)
+  int contracted = 0;                // the contracted flavour of the hot kernels (g3m3_model_set_contracted)
   float* flux_hist = nullptr;        // flux_counter history [step][box][6]
   unsigned* flux_count = nullptr;
   int flux_cap = 0;

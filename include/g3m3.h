@@ -553,6 +553,12 @@ int g3m3_model_craft_records(g3m3_model* m, float* out, int* nsteps);
  * graphs are dropped when the choice changes. */
 #define G3M3_FCS_VARIANTS 8
 int g3m3_model_set_variant(g3m3_model* m, int kernel, int variant);
+/* The contracted flavour (on = 1): the push kernels built with fused
+ * multiply-add contraction and quotients by a shared denominator taken as
+ * products with its reciprocal.  Results are no longer the reference's FP32
+ * bits; they stay within 1e-5 relative L2 per field per main step of them
+ * (tests/test_contracted_gpu.py).  Off by default. */
+int g3m3_model_set_contracted(g3m3_model* m, int on);
 int g3m3_model_autotune(g3m3_model* m, int* fcs_variant);
 /* Time bookkeeping: t, t_stepnew(1..n_grids), executed cell-updates. */
 int g3m3_model_times(g3m3_model* m, double* t, double* t_stepnew,

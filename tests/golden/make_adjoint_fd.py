@@ -29,18 +29,28 @@ import _adjoint_ref as R  # noqa: E402
 NSTEPS = 50
 
 
-def config3():
+def config3(**over):
     from g3m3_gb300.state import make_config
-    return make_config("nested", limit=48, n_grids=3)
+    return make_config("nested", limit=48, n_grids=3, **over)
 
 
-def main():
+def main(argv=()):
+    """Options (diagnostics; the fixture is made without them):
+    --divb-every N, --errlim E, --params 0,1,.. (components of u), --out NAME."""
+    opts = dict(a.split("=", 1) for a in argv if a.startswith("--"))
+    over = {}
+    if "--divb-every" in opts:
+        over["divb_every"] = int(opts["--divb-every"])
+    if "--errlim" in opts:
+        over["divb_errlim"] = float(opts["--errlim"])
+    comps = [int(x) for x in opts["--params"].split(",")] if "--params" in opts else list(range(7))
+    name = opts.get("--out", "adjoint_fd_config3.json")
     import torch
     from g3m3_gb300.adjoint import line_samples, upstream_wind
     from g3m3_gb300.state import CONFIGS, Setup
     from oracle.oracle import OracleModel
-    st = config3()
-    setup = Setup(**dict(CONFIGS["nested"], limit=48, n_grids=3))
+    st = config3(**over)
+    setup = Setup(**dict(CONFIGS["nested"], limit=48, n_grids=3, **over))
     samples = line_samples(st, NSTEPS, n=200)
     om = OracleModel(st, omp=True)
     om.init_steps()
@@ -58,7 +68,7 @@ def main():
     L0 = R.oracle_loss(st, wind(u0), sch, samples)
     print(f"loss {L0:.10e}", flush=True)
     fd = []
-    for k in range(7):
+    for k in comps:
         h = 1e-4 * scale[k]
         up, um = u0.copy(), u0.copy()
         up[k] += h
@@ -67,13 +77,14 @@ def main():
         g = (R.oracle_loss(st, wind(up), sch, samples) - R.oracle_loss(st, wind(um), sch, samples)) / (2 * h)
         fd.append(g)
         print(f"u[{k}]: {g:.8e} ({time.time() - t0:.0f} s)", flush=True)
-    out = {"config": "3 nested boxes 97x97x49, 50 main steps, div B every 10 (errlim 1e-4), 200 line samples",
+    out = {"config": "3 nested boxes 97x97x49, 50 main steps, div B every %d (errlim %g), 200 line samples"
+                     % (st.params.divb_every, st.params.divb_errlim), "components": comps,
            "u": u0.tolist(), "h_rel": 1e-4, "h": (1e-4 * scale).tolist(), "loss_fp64": L0,
            "grad_u_fd_fp64": fd, "schedule": sch}
-    with open(os.path.join(HERE, "adjoint_fd_config3.json"), "w") as fh:
+    with open(os.path.join(HERE, name), "w") as fh:
         json.dump(out, fh, indent=1)
     print("written")
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

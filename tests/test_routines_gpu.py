@@ -325,7 +325,7 @@ def test_divb_correct(cfg, errlim):
     # per component, the GPU's B is at least as close to the FP64 build's
     # (within the stated slack) as the reference's FP32 solve is
     import _divb_parity as D
-    b8, _ = D.divb_correct_r8(*I.dims(box), 7, pos, xs, errlim, *b)
+    b8, _ = D.divb_correct_r8(*I.dims(box), pos, xs, errlim, *b)
     for q in range(3):
         eg, er = D.rel(gb[q][box - 1], b8[q][box - 1]), D.rel(ob[q][box - 1], b8[q][box - 1])
         assert eg <= D.SLACK * er + D.FLOOR, (q, eg, er, it_o, it_g.value)
