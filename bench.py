@@ -194,6 +194,15 @@ def run_ours(args):
     clk = clocks.stop()
     ms_p, cu_p, k_p = timed(args.steps, not use_graph)
 
+    # the contracted flavour of push_ion (FMA contraction, reciprocal
+    # products; within 1e-5 relative L2 per field per main step of the FP32
+    # bits), same mode, then back to the bitwise build for the e2e leg
+    m.L.g3m3_model_set_contracted(m.h, 1)
+    m.run(2, graph=use_graph)                  # recaptures the step graphs
+    ms_c, cu_c, _ = timed(args.steps, use_graph)
+    m.L.g3m3_model_set_contracted(m.h, 0)
+    m.run(2, graph=use_graph)
+
     # e2e: state from pinned host memory every step, result read back
     n4 = p.n_grids * p.nz * p.ny * p.nx
     host = torch.empty((34 * n4,), dtype=torch.float32, pin_memory=True)
@@ -232,7 +241,11 @@ def run_ours(args):
     # this overwrites the wrk/old copies, so it runs after the timed legs
     rows = kernel_table(m)
     roof = roofline_from(rows)
-    (ms_g, ms_p, e2e_s), (cu_g, cu_p, cu_e, k_g) = replica_reduce([ms_g, ms_p, e2e_s], [cu_g, cu_p, cu_e, k_g])
+    m.L.g3m3_model_set_contracted(m.h, 1)
+    contracted_push = kernel_table(m, only=0)
+    m.L.g3m3_model_set_contracted(m.h, 0)
+    (ms_g, ms_p, e2e_s, ms_c), (cu_g, cu_p, cu_e, k_g, cu_c) = replica_reduce([ms_g, ms_p, e2e_s, ms_c],
+                                                                              [cu_g, cu_p, cu_e, k_g, cu_c])
     m.close()
     ctx.close()
     if rank != 0:
@@ -257,6 +270,11 @@ def run_ours(args):
                                               }[fcs_variant]}},
         "other_mode": {"value": cu_p / (ms_p / 1e3), "ms_per_step": ms_p / args.steps,
                        "mode": mode_name[not use_graph]},
+        "contracted": {"value": cu_c / (ms_c / 1e3), "ms_per_step": ms_c / args.steps,
+                       "accuracy": "push_ion with FMA contraction and reciprocal products: within 1e-5 relative "
+                                   "L2 per field per main step of the reference's FP32 bits "
+                                   "(tests/test_contracted_gpu.py)",
+                       "push_ion": contracted_push.get("push_ion")},
         "mode_trial": {"graph": trial[True] * 1e3, "streams": trial[False] * 1e3, "unit": "cell-updates/s",
                        "steps": TRIAL},
         "e2e": {"value": cu_e / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": 34 * n4 * 4,
@@ -407,6 +425,8 @@ def run_adjoint(device, nsteps=50, every=10, nsamp=200):
             "tape_bytes": tape,
             "backward_phases_s": {"rerun_with_snapshots": phases[0], "reverse_kernels": phases[1],
                                   "divb_reverse": phases[2]},
+            "backward_issue_s": {"rerun_with_snapshots": phases[3], "reverse_kernels": phases[4],
+                                 "divb_reverse": phases[5]},
             "note": "forward: the engine's graph-replayed main steps; backward: per checkpoint interval the steps "
                     "re-run with snapshots, then the reverse kernels"}
 
@@ -417,12 +437,15 @@ KERNELS = {  # id: (name, launches per box-step)
 }
 
 
-def kernel_table(m, reps=20):
-    """Each engine kernel on box 1 of the nested grid, CUDA events on the
-    engine's stream; share = launches per box-step x time per launch."""
+def kernel_table(m, reps=20, only=None):
+    """Each engine kernel (or kernel `only`) on box 1 of the nested grid,
+    CUDA events on the engine's stream; share = launches per box-step x
+    time per launch."""
     import ctypes
     rows = {}
     for kid, (name, per_step) in KERNELS.items():
+        if only is not None and kid != only:
+            continue
         ms = ctypes.c_float()
         by = ctypes.c_double()
         rc = m.L.g3m3_model_time_kernel(m.h, kid, 1, reps, ctypes.byref(ms), ctypes.byref(by))

@@ -216,11 +216,16 @@ def emit(c: Cell):
         w(f"    T {n}_b = out_b_[{i}];")
         bar[n] = f"{n}_b"
 
+    # An input's contributions are summed in a local and handed to acc_ once,
+    # right after the last of them: one accumulation (an atomic, in the
+    # scattering kernels) per input instead of one per use.
+    body_start = len(L)
+
     def add(name, expr):
         if name.startswith("T(") or name in par:
             return
         if name in inp:
-            w(f"    acc_({inp[name]}, {expr});")
+            L.append(("IN", name, expr))
         elif name in assigned:
             w(f"    {b(name)} += {expr};")
         else:
@@ -262,7 +267,29 @@ def emit(c: Cell):
             add(a[4], f"({cond} ? T(0) : {tb})")
         else:
             raise ValueError(op)
-    # silence unused-variable warnings of primal values the reverse sweep does not read
+    body = L[body_start:]
+    del L[body_start:]
+    last, count = {}, {}
+    for k, item in enumerate(body):
+        if isinstance(item, tuple):
+            last[item[1]] = k
+            count[item[1]] = count.get(item[1], 0) + 1
+    seen = set()
+    for k, item in enumerate(body):
+        if not isinstance(item, tuple):
+            w(item)
+            continue
+        _, name, expr = item
+        if count[name] == 1:
+            w(f"    acc_({inp[name]}, {expr});")
+            continue
+        if name in seen:
+            w(f"    {name}_ib += {expr};")
+        else:
+            seen.add(name)
+            w(f"    T {name}_ib = {expr};")
+        if last[name] == k:
+            w(f"    acc_({inp[name]}, {name}_ib);")
     w("  }")
     w("};")
     return "\n".join(L)

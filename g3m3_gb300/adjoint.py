@@ -84,8 +84,9 @@ class Adjoint:
 
     def phases(self):
         """Seconds of the last backward: re-run with snapshots, reverse
-        kernels, reversed div B passes."""
-        out = (ctypes.c_double * 3)()
+        kernels, reversed div B passes; then the host time spent issuing
+        each of the three."""
+        out = (ctypes.c_double * 6)()
         self.ctx.check(self.L.g3m3_adjoint_phases(self.h, out))
         return list(out)
 

@@ -182,6 +182,9 @@ struct g3m3_adjoint {
   float* a_sc = nullptr;               // [19][n3]: efld 3, cur 3, bs 3, btot, ev 3, tv 3, vt 3
   float* p1 = nullptr;                 // [34][n3]
   float* a_p1 = nullptr;               // [34][n3]
+  float* fm = nullptr;                 // [3][34][n3] each: flux-correction reverse, per face
+  float* fw = nullptr;
+  float* fp = nullptr;
   float* glist = nullptr;
   unsigned* gcount = nullptr;
   unsigned gcap = 0;
@@ -190,7 +193,8 @@ struct g3m3_adjoint {
   CgState* host_cgst = nullptr;        // pinned
   double* d_aparam = nullptr;          // [8]
   Tape tape;
-  double phase_s[3] = {};              // last backward: re-run with snapshots, reverse kernels, div B reverse
+  double phase_s[6] = {};              // last backward: re-run with snapshots, reverse kernels, div B reverse;
+                                       // then the host time spent issuing each (before the stream drained)
   bool prof = false;                   // GPU time per stage of the box-step reverses
   cudaEvent_t ev[17] = {};
   double stage_ms[16] = {};
@@ -522,7 +526,8 @@ void rev_box(g3m3_adjoint* A, const BoxRec& R) {
       f.a_old[q] = aO[q];
       f.chi[q] = q >= G3M3_F_BX ? m->p.diferg : m->p.difrho;
     }
-    f.p1 = A->p1; f.a_p1 = A->a_p1; f.nf = G3M3_NFIELDS; f.d = m->d;
+    f.p1 = A->p1; f.a_p1 = A->a_p1; f.fm = A->fm; f.fw = A->fw; f.fp = A->fp;
+    f.nf = G3M3_NFIELDS; f.d = m->d;
     mark(A, 3);
     launch_adj_fcs(f, s);
   }
@@ -564,6 +569,9 @@ void rev_box(g3m3_adjoint* A, const BoxRec& R) {
     }
     lb.nf = 4; lb.delt = R.dt; lb.d = m->d;
     launch_adj_lap(lb, s);
+    // the Lapidus reverses only read wrk's adjoint; the corrector's pushes
+    // accumulate into it next
+    cudaMemsetAsync(A->aW, 0, (size_t)G3M3_NFIELDS * n3 * sizeof(float), s);
     AdjVtotArgs v{};
     for (int sp = 0; sp < 3; sp++) {
       v.rho[sp] = c1[10 * sp];
@@ -722,8 +730,9 @@ int g3m3_adjoint_create(g3m3_model* m, int nsteps, int checkpoint_every, float c
   A->tape.block = (size_t)G3M3_NFIELDS * m->n3;
   const size_t n3 = m->n3, n4 = m->n4;
   A->gcap = (unsigned)(3 * n3 < 0xffffffffu ? 3 * n3 : 0xffffffffu);
+  const size_t nface = 3 * (size_t)G3M3_NFIELDS * n3;
   const size_t floats = 2 * (size_t)G3M3_NFIELDS * n4 + n4 + 2 * (size_t)G3M3_NFIELDS * n3 + 19 * n3 +
-                        2 * (size_t)G3M3_NFIELDS * n3 + (size_t)A->gcap * 11 + 8 * n3 +
+                        2 * (size_t)G3M3_NFIELDS * n3 + (size_t)A->gcap * 11 + 8 * n3 + 3 * nface +
                         (size_t)(A->nseg + 1) * (G3M3_NFIELDS + 1) * n4;
   cudaError_t e = dev_alloc(m->ctx, (void**)&A->mem, floats * sizeof(float));
   if (e != cudaSuccess) {
@@ -741,6 +750,9 @@ int g3m3_adjoint_create(g3m3_model* m, int nsteps, int checkpoint_every, float c
   A->a_p1 = q; q += (size_t)G3M3_NFIELDS * n3;
   A->glist = q; q += (size_t)A->gcap * 11;
   A->cgv = q; q += 8 * n3;
+  A->fm = q; q += nface;
+  A->fw = q; q += nface;
+  A->fp = q; q += nface;
   for (int i = 0; i <= A->nseg; i++) {
     A->ckpt.push_back(q);
     q += (size_t)(G3M3_NFIELDS + 1) * n4;
@@ -864,9 +876,11 @@ int g3m3_adjoint_backward(g3m3_adjoint* A, double* grad_params, float* grad_stat
   for (double& t : A->phase_s) t = 0.0;
   using clk = std::chrono::steady_clock;
   auto lap = [&](clk::time_point& t0, int phase) {   // phase time, the stream drained
+    const clk::time_point tq = clk::now();
     cudaStreamSynchronize(s);
     const clk::time_point t1 = clk::now();
     A->phase_s[phase] += std::chrono::duration<double>(t1 - t0).count();
+    A->phase_s[3 + phase] += std::chrono::duration<double>(tq - t0).count();
     t0 = t1;
   };
   clk::time_point t0 = clk::now();
@@ -948,7 +962,7 @@ int g3m3_adjoint_profile(g3m3_adjoint* A, int on, double* stage_ms) {
 
 int g3m3_adjoint_phases(g3m3_adjoint* A, double* seconds) {
   if (!A || !seconds) return G3M3_ERR_ARG;
-  for (int q = 0; q < 3; q++) seconds[q] = A->phase_s[q];
+  for (int q = 0; q < 6; q++) seconds[q] = A->phase_s[q];
   return G3M3_OK;
 }
 

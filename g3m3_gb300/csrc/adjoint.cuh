@@ -102,13 +102,16 @@ struct AdjFcsArgs {              // flux correction of nf fields
   const float* wrk[G3M3_NFIELDS];
   const float* old[G3M3_NFIELDS];
   float* p1;                     // scratch [nf][cells]: P1 = wrk + chi Lap7(old)
-  float* a_p1;                   // scratch [nf][cells], zero on entry
+  float* a_p1;                   // scratch [nf][cells]: P1's adjoint (written by the gather)
+  float* fm;                     // scratch [3][nf][cells]: per face and axis, the value its limiter
+  float* fw;                     //   passes to d1m, dw or d1p (zero for the other two)
+  float* fp;
   float* a_px[G3M3_NFIELDS];
   float* a_wrk[G3M3_NFIELDS];
   float* a_old[G3M3_NFIELDS];
   float chi[G3M3_NFIELDS];
   int nf;
-  int clear_px;                  // set by the launcher: k_adj_p1 clears a_px (the gather form)
+  int clear_px;                  // set by the launcher: k_adj_p1 clears a_px
   Dims d;
 };
 

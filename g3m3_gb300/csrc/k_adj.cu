@@ -28,14 +28,17 @@ struct Cell3 {
   bool ok, interior;
 };
 
-__device__ __forceinline__ Cell3 cell3(const Dims& d) {
+__device__ __forceinline__ Cell3 cell3(const Dims& d) {   // one thread per cell, x fastest, 1D blocks
   Cell3 r;
-  r.i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  r.j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  r.k = blockIdx.z * blockDim.z + threadIdx.z + 1;
-  r.ok = r.i <= d.nx && r.j <= d.ny && r.k <= d.nz;
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  r.ok = t < (long)d.nx * d.ny * d.nz;
+  const long tt = r.ok ? t : 0;
+  const long u = tt / d.nx;
+  r.i = (int)(tt - u * d.nx) + 1;
+  r.j = (int)(u % d.ny) + 1;
+  r.k = (int)(u / d.ny) + 1;
   r.interior = r.i > 1 && r.j > 1 && r.k > 1 && r.i < d.nx && r.j < d.ny && r.k < d.nz;
-  r.c = r.ok ? d.at(r.i, r.j, r.k) : 0;
+  r.c = (size_t)tt;
   return r;
 }
 
@@ -343,64 +346,92 @@ __global__ void __launch_bounds__(256) k_adj_curl(const __grid_constant__ AdjFie
 }
 
 // ------------------------------------------------------------ Lapidus
+// The smoothing of a field f at an interior cell c (sub_lap_plasma.f90:
+// 50-140, sub_lap_elec.f90:33-48) is
+//   out(c) = f(c) + chi delt sum_e [U(c,c+e) (f(c+e) - f(c)) - U(c-e,c) (f(c) - f(c-e))],
+// U(a,b) = |v_e(b) - v_e(a)| the jump of the velocity component e across
+// the face (a, b) (lap_speed_cell / lap_jump_cell: the same value from both
+// sides).  A face (a, b = a + e) adds k F to out(a) and -k F to out(b),
+// F = U (f(b) - f(a)), k = chi delt, where those cells are interior.  Its
+// adjoint is Fbar = k (I(a) abar(a) - I(b) abar(b)) (I: interior), passing
+// -U Fbar to fbar(a), U Fbar to fbar(b) and Fbar (f(b) - f(a)) to U; seen
+// from a cell c and a neighbour n across either face this is the same
+// expression, D = I(c) abar(c) - I(n) abar(n): fbar(c) -= U k D,
+// Ubar += k D (f(n) - f(c)), vbar_e(c) += sign(v_e(c) - v_e(n)) Ubar.  So
+// every cell gathers its six faces' shares and its own identity term, with
+// no atomics, and turns its velocity adjoint into the adjoints of its own
+// rho and p (v = p / max(rho, floor)) or adds it to the given velocity's.
+// The output adjoints are only read: the caller clears them afterwards.
+template <int NF>   // fields of the call at most (10: a species, 4: epres and B)
 __global__ void __launch_bounds__(128) k_adj_lap(const __grid_constant__ AdjLapArgs a) {
   const Dims d = a.d;
   const Cell3 p = cell3(d);
-  if (!p.ok || !p.interior) return;
+  if (!p.ok) return;
   const size_t c = p.c;
-  float gout[10];
-  bool any = false;
-  for (int f = 0; f < a.nf; f++) {
-    gout[f] = a.a_out[f][c];
-    any |= gout[f] != 0.0f;
-    a.a_out[f][c] = 0.0f;
-  }
-  if (!any) return;
-  const Off7 o(d);
-  using Cs = adj::lap_speed_cell<float>;
-  using Cj = adj::lap_jump_cell<float>;
-  using Cf = adj::lap_field_cell<float>;
-  float vin[Cs::NIN];
-  float u[6];
-  if (a.vrho) {
-    for (int q = 0; q < 7; q++) vin[q] = __ldg(a.vrho + c + o.o[q]);
-    vin[7] = __ldg(a.vp[0] + c); vin[8] = __ldg(a.vp[0] + c + o.o[1]); vin[9] = __ldg(a.vp[0] + c + o.o[2]);
-    vin[10] = __ldg(a.vp[1] + c); vin[11] = __ldg(a.vp[1] + c + o.o[3]); vin[12] = __ldg(a.vp[1] + c + o.o[4]);
-    vin[13] = __ldg(a.vp[2] + c); vin[14] = __ldg(a.vp[2] + c + o.o[5]); vin[15] = __ldg(a.vp[2] + c + o.o[6]);
-    const float vpar[1] = {a.vfloor};
-    Cs::fwd(vin, vpar, u);
+  const int idx[3] = {p.i, p.j, p.k};
+  const int nn[3] = {d.nx, d.ny, d.nz};
+  const long st[3] = {1, (long)d.nx, (long)d.nx * d.ny};
+  bool in[3];
+  for (int e = 0; e < 3; e++) in[e] = idx[e] > 1 && idx[e] < nn[e];
+  const bool ic = in[0] && in[1] && in[2];
+  const bool species = a.vrho != nullptr;
+  // velocity at c (all components) and of a neighbour (one component)
+  float r0 = 0.0f, v0[3];
+  if (species) {
+    r0 = amax1(__ldg(a.vrho + c), a.vfloor);
+    for (int e = 0; e < 3; e++) v0[e] = __ldg(a.vp[e] + c) / r0;
   } else {
-    vin[0] = __ldg(a.v[0] + c); vin[1] = __ldg(a.v[0] + c + o.o[1]); vin[2] = __ldg(a.v[0] + c + o.o[2]);
-    vin[3] = __ldg(a.v[1] + c); vin[4] = __ldg(a.v[1] + c + o.o[3]); vin[5] = __ldg(a.v[1] + c + o.o[4]);
-    vin[6] = __ldg(a.v[2] + c); vin[7] = __ldg(a.v[2] + c + o.o[5]); vin[8] = __ldg(a.v[2] + c + o.o[6]);
-    Cj::fwd(vin, nullptr, u);
+    for (int e = 0; e < 3; e++) v0[e] = __ldg(a.v[e] + c);
   }
-  float ub[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-  for (int f = 0; f < a.nf; f++) {
-    if (gout[f] == 0.0f) continue;
-    float in[Cf::NIN];
-    for (int q = 0; q < 7; q++) in[q] = __ldg(a.in[f] + c + o.o[q]);
-    for (int q = 0; q < 6; q++) in[7 + q] = u[q];
-    const float par[2] = {a.chi[f], a.delt};
-    float* ain = a.a_in[f];
-    Cf::adj(in, par, &gout[f], [&](int s, float v) {
-      if (s < 7) red(ain + c + o.o[s], v);
-      else ub[s - 7] += v;
-    });
+  auto vel = [&](int e, size_t q) {
+    return species ? __ldg(a.vp[e] + q) / amax1(__ldg(a.vrho + q), a.vfloor) : __ldg(a.v[e] + q);
+  };
+  float ga[NF], fc[NF], acc[NF];
+#pragma unroll
+  for (int f = 0; f < NF; f++) {
+    const bool on = f < a.nf;
+    ga[f] = on && ic ? __ldg(a.a_out[f] + c) : 0.0f;
+    fc[f] = on ? __ldg(a.in[f] + c) : 0.0f;
+    acc[f] = ga[f];
   }
-  if (a.vrho) {
-    const float vpar[1] = {a.vfloor};
-    Cs::adj(vin, vpar, ub, [&](int s, float v) {
-      if (s < 7) red(a.a_vrho + c + o.o[s], v);
-      else if (s < 10) red(a.a_vp[0] + c + o.o[s == 7 ? 0 : (s == 8 ? 1 : 2)], v);
-      else if (s < 13) red(a.a_vp[1] + c + o.o[s == 10 ? 0 : (s == 11 ? 3 : 4)], v);
-      else red(a.a_vp[2] + c + o.o[s == 13 ? 0 : (s == 14 ? 5 : 6)], v);
-    });
+  float vb[3] = {0.0f, 0.0f, 0.0f};
+  for (int e = 0; e < 3; e++) {
+    const bool others = (e == 0 || in[0]) && (e == 1 || in[1]) && (e == 2 || in[2]);
+    for (int dir = -1; dir <= 1; dir += 2) {
+      const int t = idx[e] + dir;
+      if (t < 1 || t > nn[e]) continue;
+      const bool inb = others && t > 1 && t < nn[e];
+      if (!ic && !inb) continue;
+      const size_t q = (size_t)((long)c + dir * st[e]);
+      const float vn = vel(e, q);
+      const float u = fabsf(v0[e] - vn);
+      float ub = 0.0f;
+#pragma unroll
+      for (int f = 0; f < NF; f++) {
+        if (f >= a.nf) continue;
+        const float dd = ga[f] - (inb ? __ldg(a.a_out[f] + q) : 0.0f);
+        if (dd == 0.0f) continue;
+        const float kd = a.chi[f] * a.delt * dd;
+        acc[f] -= u * kd;
+        ub += kd * (__ldg(a.in[f] + q) - fc[f]);
+      }
+      vb[e] += sgn(v0[e] - vn) * ub;
+    }
+  }
+#pragma unroll
+  for (int f = 0; f < NF; f++)
+    if (f < a.nf && acc[f] != 0.0f) a.a_in[f][c] += acc[f];
+  if (species) {
+    float rb = 0.0f;
+    for (int e = 0; e < 3; e++) {
+      if (vb[e] == 0.0f) continue;
+      a.a_vp[e][c] += vb[e] / r0;
+      rb -= vb[e] * v0[e] / r0;
+    }
+    if (rb != 0.0f && __ldg(a.vrho + c) > a.vfloor) a.a_vrho[c] += rb;
   } else {
-    Cj::adj(vin, nullptr, ub, [&](int s, float v) {
-      const int q = s / 3, r = s % 3;   // component, point (c, +, -)
-      red(a.a_v[q] + c + o.o[r == 0 ? 0 : 1 + 2 * q + (r - 1)], v);
-    });
+    for (int e = 0; e < 3; e++)
+      if (vb[e] != 0.0f) a.a_v[e][c] += vb[e];
   }
 }
 
@@ -430,11 +461,10 @@ __global__ void __launch_bounds__(256) k_adj_vtot(const __grid_constant__ AdjVto
 __global__ void __launch_bounds__(256) k_fcs_p1(const __grid_constant__ AdjFcsArgs a) {
   const Dims d = a.d;
   const Cell3 p = cell3(d);
-  const int f = blockIdx.z / ((d.nz + blockDim.z - 1) / blockDim.z);
-  if (f >= a.nf) return;
-  const int k = (blockIdx.z % ((d.nz + blockDim.z - 1) / blockDim.z)) * blockDim.z + threadIdx.z + 1;
-  if (p.i > d.nx || p.j > d.ny || k > d.nz) return;
-  const size_t c = d.at(p.i, p.j, k);
+  const int f = blockIdx.y;
+  if (!p.ok || f >= a.nf) return;
+  const int k = p.k;
+  const size_t c = p.c;
   const size_t n = d.cells();
   const float* W = a.wrk[f];
   const float* O = a.old[f];
@@ -445,122 +475,115 @@ __global__ void __launch_bounds__(256) k_fcs_p1(const __grid_constant__ AdjFcsAr
                         + __ldg(O + c + sz) + __ldg(O + c - sz) - 6.0f * __ldg(O + c));
   }
   a.p1[(size_t)f * n + c] = v;
-  a.a_p1[(size_t)f * n + c] = 0.0f;
 }
 
+// The flux-correction reverse in two passes, without atomics.  Along an
+// axis, the limiter flux of face m (2 <= m <= n-1; the reference clamps the
+// end faces onto these, sub_fcsmooth.f90:87-239)
+//   fn = s max(0, min(s d1m, chi |dw|, s d1p)),  s = sign(dw),
+//   d1m = P1(m) - P1(m-1), d1p = P1(q+1) - P1(q), dw = W(m+1) - W(m),
+//   q = min(m+1, n-1),
+// enters output cell m with -1, cell m+1 with +1 (m+1 <= n-1) and, for
+// m = 2, cell 2 once more with +1 (cell 2's lower face is clamped onto face
+// 2); on x and y only in interior k planes.  So its adjoint is
+// g = -A(m) + A(m+1) [m+1 <= n-1] + A(2) [m = 2], A the output's adjoint,
+// and the limiter passes g to exactly one of the three differences, the one
+// the min/max chose (none where 0 won; the ties as the forward breaks them,
+// amin1/amax1).  k_adj_fcs_faces evaluates every face once and stores the
+// passed value in one of three arrays, by the difference it goes to (d1m,
+// dw, d1p; zeros elsewhere and at positions that are no face);
+// k_adj_fcs_gather then adds to each point, with loads that do not depend
+// on the limiter's choices, the shares of the four faces along each axis
+// whose differences hold it, plus the output's own adjoint (to P1 where the
+// output is P1 - fluxes, to W where it is W).
 template <int AX>
-__device__ __forceinline__ void fcs_flux_adj(const AdjFcsArgs& a, int f, int i, int j, int k, int m, float g) {
-  if (g == 0.0f) return;
+__device__ __forceinline__ void fcs_face(const AdjFcsArgs& a, int f, int i, int j, int k) {
   const Dims& d = a.d;
   const int n = AX == 0 ? d.nx : (AX == 1 ? d.ny : d.nz);
-  m = clampi(m, 2, n - 1);
-  const int q = m + 1 > n - 1 ? n - 1 : m + 1;
+  const int m = AX == 0 ? i : (AX == 1 ? j : k);
   auto at = [&](int t) { return AX == 0 ? d.at(t, j, k) : (AX == 1 ? d.at(i, t, k) : d.at(i, j, t)); };
   const size_t cells = d.cells();
-  const float* P = a.p1 + (size_t)f * cells;
-  const float* W = a.wrk[f];
-  const size_t idx[6] = {at(m - 1), at(m), at(q), at(q + 1), at(m), at(m + 1)};
-  float in[6];
-  for (int t = 0; t < 4; t++) in[t] = __ldg(P + idx[t]);
-  in[4] = __ldg(W + idx[4]);
-  in[5] = __ldg(W + idx[5]);
-  const float par[1] = {a.chi[f]};
-  float* AP = a.a_p1 + (size_t)f * cells;
-  float* AW = a.a_wrk[f];
-  adj::fcs_flux_cell<float>::adj(in, par, &g, [&](int s, float v) {
-    if (s < 4) red(AP + idx[s], v);
-    else red(AW + idx[s], v);
-  });
+  const size_t slot = ((size_t)AX * a.nf + f) * cells + at(m);
+  float vm = 0.0f, vw = 0.0f, vp = 0.0f;   // to d1m, dw, d1p
+  if (m >= 2 && m <= n - 1 && (AX == 2 || (k != 1 && k != d.nz))) {
+    const float* Apx = a.a_px[f];
+    float g = -__ldg(Apx + at(m));
+    if (m + 1 <= n - 1) g += __ldg(Apx + at(m + 1));
+    if (m == 2) g += __ldg(Apx + at(2));
+    if (g != 0.0f) {
+      const float* P = a.p1 + (size_t)f * cells;
+      const float* W = a.wrk[f];
+      const int q = m + 1 > n - 1 ? n - 1 : m + 1;
+      const float chi = a.chi[f];
+      const float dw = __ldg(W + at(m + 1)) - __ldg(W + at(m));
+      const float sg = dw >= 0.0f ? 1.0f : -1.0f;
+      const float tm = sg * (__ldg(P + at(m)) - __ldg(P + at(m - 1)));
+      const float tw = chi * fabsf(dw);
+      const float tp = sg * (__ldg(P + at(q + 1)) - __ldg(P + at(q)));
+      const bool c1m = tm < tw;                 // amin1(s d1m, chi |dw|)
+      const float v1 = c1m ? tm : tw;
+      const bool c2p = !(v1 < tp);              // amin1(., s d1p)
+      const float v2 = c2p ? tp : v1;
+      if (!(0.0f > v2)) {                       // amax1(0, .): the zero passes nothing
+        if (c2p) vp = g;                        // d(s s d1p)/d(d1p) = 1
+        else if (c1m) vm = g;
+        else vw = g * chi * sg * sgn(dw);
+      }
+    }
+  }
+  a.fm[slot] = vm;
+  a.fw[slot] = vw;
+  a.fp[slot] = vp;
 }
 
-__global__ void __launch_bounds__(256) k_adj_fcs(const __grid_constant__ AdjFcsArgs a) {
+__global__ void __launch_bounds__(256) k_adj_fcs_faces(const __grid_constant__ AdjFcsArgs a) {
   const Dims d = a.d;
   const Cell3 p = cell3(d);
-  const int zb = (d.nz + blockDim.z - 1) / blockDim.z;
-  const int f = blockIdx.z / zb;
-  if (f >= a.nf) return;
-  const int i = p.i, j = p.j;
-  const int k = (blockIdx.z % zb) * blockDim.z + threadIdx.z + 1;
-  if (i > d.nx || j > d.ny || k > d.nz) return;
-  const size_t c = d.at(i, j, k);
-  const float g = a.a_px[f][c];
-  a.a_px[f][c] = 0.0f;
-  if (g == 0.0f) return;
-  if (k == 1 || k == d.nz) {
-    red(a.a_wrk[f] + c, g);
-    return;
-  }
-  if (i == 1 || i == d.nx) {
-    red(a.a_wrk[f] + c, g);
-  } else {
-    red(a.a_p1 + (size_t)f * d.cells() + c, g);
-    fcs_flux_adj<0>(a, f, i, j, k, i, -g);
-    fcs_flux_adj<0>(a, f, i, j, k, i - 1, g);
-  }
-  if (j != 1 && j != d.ny) {
-    fcs_flux_adj<1>(a, f, i, j, k, j, -g);
-    fcs_flux_adj<1>(a, f, i, j, k, j - 1, g);
-  }
-  fcs_flux_adj<2>(a, f, i, j, k, k, -g);
-  fcs_flux_adj<2>(a, f, i, j, k, k - 1, g);
+  const int f = blockIdx.y;
+  if (!p.ok || f >= a.nf) return;
+  const int i = p.i, j = p.j, k = p.k;
+  fcs_face<0>(a, f, i, j, k);
+  fcs_face<1>(a, f, i, j, k);
+  fcs_face<2>(a, f, i, j, k);
 }
 
-// The same reverse as a gather, without atomics.  Along each axis the flux
-// at face m (2 <= m <= n-1; the reference clamps end faces onto these)
-// enters output cell m with -1, cell m+1 with +1 (m+1 <= n-1) and, for
-// m = 2, cell 2 once more with +1 (cell 2's lower face is clamped onto
-// face 2).  So a face's adjoint is a combination of the outputs' adjoints
-// around it, and a point's share of the faces that read it (faces m-2 ..
-// m+1) is gathered by the thread of that point.  The thread then holds the
-// whole adjoint of P1 at its cell (stored) and the flux and direct parts of
-// wrk's (added); k_adj_p1 finishes with P1's dependence on wrk and old.
+// The shares at point p of one axis: d1m of face m adds to P(m), subtracts
+// from P(m-1); d1p of face m adds to P(q+1), subtracts from P(q) (q = m+1,
+// or m for the clamped face m = n-1); dw adds to W(m+1), subtracts from
+// W(m).  Faces that do not exist hold zeros.
 template <int AX>
-__device__ __forceinline__ void fcs_axis_gather(const AdjFcsArgs& a, int f, int i, int j, int k, float& accP,
+__device__ __forceinline__ void fcs_gather_axis(const AdjFcsArgs& a, int f, int i, int j, int k, float& accP,
                                                 float& accW) {
   const Dims& d = a.d;
   const int n = AX == 0 ? d.nx : (AX == 1 ? d.ny : d.nz);
   const int p = AX == 0 ? i : (AX == 1 ? j : k);
+  if (AX != 2 && (k == 1 || k == d.nz)) return;
   auto at = [&](int t) { return AX == 0 ? d.at(t, j, k) : (AX == 1 ? d.at(i, t, k) : d.at(i, j, t)); };
-  const float* Apx = a.a_px[f];
-  // the pass of this axis runs for cells off the k faces (x, y) or for all
-  // cells of an interior k plane (z)
-  const bool pass = AX == 2 ? true : (k != 1 && k != d.nz);
-  if (!pass) return;
-  auto A = [&](int t) { return __ldg(Apx + at(t)); };
-  const size_t cells = d.cells();
-  const float* P = a.p1 + (size_t)f * cells;
-  const float* W = a.wrk[f];
-  const float par[1] = {a.chi[f]};
-  const int m_lo = p - 2 > 2 ? p - 2 : 2;
-  const int m_hi = p + 1 < n - 1 ? p + 1 : n - 1;
-  for (int m = m_lo; m <= m_hi; m++) {
-    float g = -A(m);
-    if (m + 1 <= n - 1) g += A(m + 1);
-    if (m == 2) g += A(2);
-    if (g == 0.0f) continue;
-    const int q = m + 1 > n - 1 ? n - 1 : m + 1;
-    const int idx[6] = {m - 1, m, q, q + 1, m, m + 1};
-    float in[6];
-    for (int t = 0; t < 4; t++) in[t] = __ldg(P + at(idx[t]));
-    in[4] = __ldg(W + at(idx[4]));
-    in[5] = __ldg(W + at(idx[5]));
-    adj::fcs_flux_cell<float>::adj(in, par, &g, [&](int s, float v) {
-      if (idx[s] != p) return;
-      if (s < 4) accP += v;
-      else accW += v;
-    });
-  }
+  const size_t base = ((size_t)AX * a.nf + f) * d.cells();
+  const float* FM = a.fm + base;
+  const float* FW = a.fw + base;
+  const float* FP = a.fp + base;
+  const size_t c = at(p);
+  const long st = AX == 0 ? 1L : (AX == 1 ? (long)d.nx : (long)d.nx * d.ny);
+  const float m0 = FM[c];
+  const float m1 = p + 1 <= n ? FM[c + st] : 0.0f;
+  const float w0 = FW[c];
+  const float w1 = p >= 2 ? FW[c - st] : 0.0f;
+  const float p2 = p >= 3 ? FP[c - 2 * st] : 0.0f;             // face p-2 (q + 1 = p)
+  const float p1 = p >= 2 && p <= n - 1 ? FP[c - st] : 0.0f;    // face p-1 (q = p)
+  float pe = 0.0f;                                               // the clamped face n-1
+  if (p == n) pe = FP[c - st];
+  else if (p == n - 1) pe = -FP[c];
+  accP += m0 - m1 + p2 - p1 + pe;
+  accW += w1 - w0;
 }
 
 __global__ void __launch_bounds__(256) k_adj_fcs_gather(const __grid_constant__ AdjFcsArgs a) {
   const Dims d = a.d;
   const Cell3 p = cell3(d);
-  const int zb = (d.nz + blockDim.z - 1) / blockDim.z;
-  const int f = blockIdx.z / zb;
-  if (f >= a.nf) return;
-  const int i = p.i, j = p.j;
-  const int k = (blockIdx.z % zb) * blockDim.z + threadIdx.z + 1;
-  if (i > d.nx || j > d.ny || k > d.nz) return;
+  const int f = blockIdx.y;
+  if (!p.ok || f >= a.nf) return;
+  const int i = p.i, j = p.j, k = p.k;
   const size_t c = d.at(i, j, k);
   float accP = 0.0f, accW = 0.0f;
   const float g = __ldg(a.a_px[f] + c);
@@ -568,9 +591,9 @@ __global__ void __launch_bounds__(256) k_adj_fcs_gather(const __grid_constant__ 
   else accP += g;                                              // t = P1
   // every point gathers along every axis: a boundary point is read by the
   // faces next to it even where its own cell takes no flux
-  fcs_axis_gather<0>(a, f, i, j, k, accP, accW);
-  fcs_axis_gather<1>(a, f, i, j, k, accP, accW);
-  fcs_axis_gather<2>(a, f, i, j, k, accP, accW);
+  fcs_gather_axis<0>(a, f, i, j, k, accP, accW);
+  fcs_gather_axis<1>(a, f, i, j, k, accP, accW);
+  fcs_gather_axis<2>(a, f, i, j, k, accP, accW);
   a.a_p1[(size_t)f * d.cells() + c] = accP;
   if (accW != 0.0f) a.a_wrk[f][c] += accW;
 }
@@ -579,12 +602,9 @@ __global__ void __launch_bounds__(256) k_adj_fcs_gather(const __grid_constant__ 
 __global__ void __launch_bounds__(256) k_adj_p1(const __grid_constant__ AdjFcsArgs a) {
   const Dims d = a.d;
   const Cell3 p = cell3(d);
-  const int zb = (d.nz + blockDim.z - 1) / blockDim.z;
-  const int f = blockIdx.z / zb;
-  if (f >= a.nf) return;
-  const int i = p.i, j = p.j;
-  const int k = (blockIdx.z % zb) * blockDim.z + threadIdx.z + 1;
-  if (i > d.nx || j > d.ny || k > d.nz) return;
+  const int f = blockIdx.y;
+  if (!p.ok || f >= a.nf) return;
+  const int i = p.i, j = p.j, k = p.k;
   const size_t c = d.at(i, j, k);
   const float* G = a.a_p1 + (size_t)f * d.cells();
   const float g = G[c];
@@ -1289,7 +1309,8 @@ __global__ void k_axpy(float* y, const float* __restrict__ x, size_t n) {
     y[c] += x[c];
 }
 
-inline dim3 cells_grid(const Dims& d, const dim3& b) { return grid3(d, b); }
+inline dim3 cells_grid(const Dims& d, const dim3& b) { return dim3(blocks_for(d.cells(), b.x * b.y * b.z)); }
+inline unsigned tcount(const dim3& b) { return b.x * b.y * b.z; }
 
 }  // namespace
 
@@ -1299,26 +1320,27 @@ void launch_adj_push_ion(const AdjPushIonArgs& a, cudaStream_t s) {
     k_adj_push_ion_shell<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
   }
   const dim3 blk(32, 2, 2);
-  k_adj_push_ion<<<cells_grid(a.d, blk), blk, 0, s>>>(a);
+  k_adj_push_ion<<<cells_grid(a.d, blk), tcount(blk), 0, s>>>(a);
 }
 
 void launch_adj_push_field(const AdjPushFieldArgs& a, cudaStream_t s) {
   const dim3 blk(32, 4, 2);
-  k_adj_push_field<<<cells_grid(a.d, blk), blk, 0, s>>>(a);
+  k_adj_push_field<<<cells_grid(a.d, blk), tcount(blk), 0, s>>>(a);
 }
 
 void launch_adj_fields(const AdjFieldsArgs& a, cudaStream_t s) {
   const dim3 blk(32, 4, 2);
   const unsigned pw = blocks_for(a.d.cells(), 256) < 8u * sm_count() ? blocks_for(a.d.cells(), 256) : 8u * sm_count();
-  k_adj_bande<<<cells_grid(a.d, blk), blk, 0, s>>>(a);
+  k_adj_bande<<<cells_grid(a.d, blk), tcount(blk), 0, s>>>(a);
   k_adj_evel<<<pw, 256, 0, s>>>(a);
   k_adj_total_b<<<pw, 256, 0, s>>>(a);
-  k_adj_curl<<<cells_grid(a.d, blk), blk, 0, s>>>(a);
+  k_adj_curl<<<cells_grid(a.d, blk), tcount(blk), 0, s>>>(a);
 }
 
 void launch_adj_lap(const AdjLapArgs& a, cudaStream_t s) {
   const dim3 blk(32, 2, 2);
-  k_adj_lap<<<cells_grid(a.d, blk), blk, 0, s>>>(a);
+  if (a.nf <= 4) k_adj_lap<4><<<cells_grid(a.d, blk), tcount(blk), 0, s>>>(a);
+  else k_adj_lap<10><<<cells_grid(a.d, blk), tcount(blk), 0, s>>>(a);
 }
 
 void launch_adj_vtot(const AdjVtotArgs& a, cudaStream_t s) {
@@ -1326,26 +1348,11 @@ void launch_adj_vtot(const AdjVtotArgs& a, cudaStream_t s) {
   k_adj_vtot<<<pw, 256, 0, s>>>(a);
 }
 
-// the scatter form (atomic reductions of every flux's contributions): the
-// direct statement, kept to check the gather form against
-void launch_adj_fcs_scatter(const AdjFcsArgs& a, cudaStream_t s) {
-  const dim3 blk(32, 4, 2);
-  const unsigned zb = (unsigned)((a.d.nz + blk.z - 1) / blk.z);
-  const dim3 grd((unsigned)((a.d.nx + blk.x - 1) / blk.x), (unsigned)((a.d.ny + blk.y - 1) / blk.y),
-                 zb * (unsigned)a.nf);
-  AdjFcsArgs b = a;
-  b.clear_px = 0;
-  k_fcs_p1<<<grd, blk, 0, s>>>(b);
-  k_adj_fcs<<<grd, blk, 0, s>>>(b);
-  k_adj_p1<<<grd, blk, 0, s>>>(b);
-}
-
 void launch_adj_fcs(const AdjFcsArgs& a, cudaStream_t s) {
-  const dim3 blk(32, 4, 2);
-  const unsigned zb = (unsigned)((a.d.nz + blk.z - 1) / blk.z);
-  const dim3 grd((unsigned)((a.d.nx + blk.x - 1) / blk.x), (unsigned)((a.d.ny + blk.y - 1) / blk.y),
-                 zb * (unsigned)a.nf);
+  const unsigned blk = 256;
+  const dim3 grd(blocks_for(a.d.cells(), blk), (unsigned)a.nf);
   k_fcs_p1<<<grd, blk, 0, s>>>(a);
+  k_adj_fcs_faces<<<grd, blk, 0, s>>>(a);
   AdjFcsArgs b = a;
   b.clear_px = 1;
   k_adj_fcs_gather<<<grd, blk, 0, s>>>(b);
@@ -1355,7 +1362,7 @@ void launch_adj_fcs(const AdjFcsArgs& a, cudaStream_t s) {
 void launch_adj_guard(const AdjGuardArgs& a, cudaStream_t s) {
   const dim3 blk(32, 2, 2);
   cudaMemsetAsync(a.list_count, 0, sizeof(unsigned), s);
-  k_adj_guard_a<<<cells_grid(a.d, blk), blk, 0, s>>>(a);
+  k_adj_guard_a<<<cells_grid(a.d, blk), tcount(blk), 0, s>>>(a);
   k_adj_guard_b<<<sm_count(), 128, 0, s>>>(a);
 }
 
@@ -1388,12 +1395,12 @@ void launch_adj_synced(const AdjSyncedArgs& a, cudaStream_t s) {
 
 void launch_adj_divb_rhs(const AdjDivbArgs& a, cudaStream_t s) {
   const dim3 blk(32, 4, 2);
-  k_adj_divb_rhs<<<cells_grid(a.d, blk), blk, 0, s>>>(a);
+  k_adj_divb_rhs<<<cells_grid(a.d, blk), tcount(blk), 0, s>>>(a);
 }
 
 void launch_adj_divb_apply(const AdjDivbArgs& a, cudaStream_t s) {
   const dim3 blk(32, 4, 2);
-  k_adj_divb_apply<<<cells_grid(a.d, blk), blk, 0, s>>>(a);
+  k_adj_divb_apply<<<cells_grid(a.d, blk), tcount(blk), 0, s>>>(a);
 }
 
 void launch_loss(const LossArgs& a, cudaStream_t s, bool reverse) {

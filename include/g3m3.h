@@ -425,7 +425,8 @@ int g3m3_adjoint_backward(g3m3_adjoint* a, double* grad_params,
 size_t g3m3_adjoint_tape_bytes(g3m3_adjoint* a);
 /* Wall-clock seconds of the last backward's phases: [0] the re-run of the
  * steps with snapshots, [1] the reverse kernels, [2] the reversed div B
- * passes (their adjoint solves). */
+ * passes (their adjoint solves); [3..5] the host time spent issuing each
+ * phase's work, before the stream drained (seconds has 6 entries). */
 int g3m3_adjoint_phases(g3m3_adjoint* a, double* seconds);
 /* Per-stage GPU time of the box-step reverses (CUDA events between the
  * stages; on = 1 turns it on for the next backward, which then waits for

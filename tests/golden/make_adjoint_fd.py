@@ -3,17 +3,27 @@ config 3 (TEST INFRASTRUCTURE): 50 main steps of 3 nested boxes of
 97x97x49, div B every 10 steps, 200 samples along the seeded line of
 g3m3_gb300.adjoint.line_samples.  The time-step schedule is the oracle's
 FP32 run's (the reference's FP32 bits); the misfit is evaluated with the
-oracle's FP64 build under that schedule and differenced with respect to
-the seven upstream conditions u = (n, vx, vy, vz, bx, by, bz) at
-h = 1e-4 relative to the magnitude of u's density, speed and field.
+oracle's FP64 build under that schedule.
+
+The differences are taken in the eight wind-face parameters w (srho, spx,
+spy, spz, spress, sbx/sby/sbz_wind), which the reference holds in FP32:
+w_k +- h_k rounded to FP32, divided by the rounded difference, so that the
+step is exact.  h_k = h_rel * scale_k, scale_k the magnitude of the
+parameter's group (srho; |sp|; spress; |sb|).  The gradient with respect
+to the upstream conditions u = (n, v, B) follows by the chain rule through
+the exact Jacobian of g3m3_gb300.adjoint.upstream_wind.  Two steps are
+taken: h_rel = 1e-4 (BASELINE config 3's) and 1e-5; the misfit has kinks
+(limiter and guard branches), and the difference quotients of the two
+steps differ by more than the smaller one differs from the adjoint.
+
 Writes adjoint_fd_config3.json beside this file; the GPU test
 tests/test_adjoint_gpu.py::test_config3_gradient compares the library's
 adjoint with it.
 
-    python tests/golden/make_adjoint_fd.py
+    python tests/golden/make_adjoint_fd.py [--params 0,1,..] [--hrel 1e-4,1e-5]
+                                           [--divb-every N] [--errlim E] [--out NAME]
 """
 import json
-import math
 import os
 import sys
 import time
@@ -34,23 +44,31 @@ def config3(**over):
     return make_config("nested", limit=48, n_grids=3, **over)
 
 
+def wind_steps(w, h_rel):
+    """The FP32-exact pairs (w_k + h, w_k - h) of every parameter."""
+    sp = np.linalg.norm(w[1:4])
+    sb = np.linalg.norm(w[5:8])
+    scale = np.array([abs(w[0]), sp, sp, sp, abs(w[4]), sb, sb, sb])
+    out = []
+    for k in range(8):
+        h = h_rel * scale[k]
+        out.append((float(np.float32(w[k] + h)), float(np.float32(w[k] - h))))
+    return out
+
+
 def main(argv=()):
-    """Options (diagnostics; the fixture is made without them):
-    --divb-every N, --errlim E, --params 0,1,.. (components of u), --out NAME."""
     opts = dict(a.split("=", 1) for a in argv if a.startswith("--"))
     over = {}
     if "--divb-every" in opts:
         over["divb_every"] = int(opts["--divb-every"])
     if "--errlim" in opts:
         over["divb_errlim"] = float(opts["--errlim"])
-    comps = [int(x) for x in opts["--params"].split(",")] if "--params" in opts else list(range(7))
+    comps = [int(x) for x in opts["--params"].split(",")] if "--params" in opts else list(range(8))
+    hrels = [float(x) for x in opts["--hrel"].split(",")] if "--hrel" in opts else [1e-4, 1e-5]
     name = opts.get("--out", "adjoint_fd_config3.json")
-    import torch
-    from g3m3_gb300.adjoint import line_samples, upstream_wind
-    from g3m3_gb300.state import CONFIGS, Setup
+    from g3m3_gb300.adjoint import line_samples, wind_of
     from oracle.oracle import OracleModel
     st = config3(**over)
-    setup = Setup(**dict(CONFIGS["nested"], limit=48, n_grids=3, **over))
     samples = line_samples(st, NSTEPS, n=200)
     om = OracleModel(st, omp=True)
     om.init_steps()
@@ -60,27 +78,23 @@ def main(argv=()):
         sch.append([float(om.s.t_stepnew[b]) for b in range(st.params.n_grids)])
         assert om.main_step() == 0
     print(f"schedule: {time.time() - t0:.0f} s", flush=True)
-    w = setup.wind
-    u0 = np.array([w.n_cm3, w.speed_kms, 0.0, 0.0, 0.0, w.b_nT * math.sin(w.clock_angle),
-                   w.b_nT * math.cos(w.clock_angle)])
-    scale = np.array([abs(u0[0])] + [np.linalg.norm(u0[1:4])] * 3 + [np.linalg.norm(u0[4:7])] * 3)
-    wind = lambda u: upstream_wind(torch.tensor(u, dtype=torch.float64), setup).numpy()
-    L0 = R.oracle_loss(st, wind(u0), sch, samples)
+    w0 = wind_of(st.params)
+    L0 = R.oracle_loss(st, w0, sch, samples)
     print(f"loss {L0:.10e}", flush=True)
-    fd = []
-    for k in comps:
-        h = 1e-4 * scale[k]
-        up, um = u0.copy(), u0.copy()
-        up[k] += h
-        um[k] -= h
-        t0 = time.time()
-        g = (R.oracle_loss(st, wind(up), sch, samples) - R.oracle_loss(st, wind(um), sch, samples)) / (2 * h)
-        fd.append(g)
-        print(f"u[{k}]: {g:.8e} ({time.time() - t0:.0f} s)", flush=True)
+    grads = {}
+    for hr in hrels:
+        pairs = wind_steps(w0, hr)
+        g = {}
+        for k in comps:
+            wp, wm = w0.copy(), w0.copy()
+            wp[k], wm[k] = pairs[k]
+            t0 = time.time()
+            g[k] = (R.oracle_loss(st, wp, sch, samples) - R.oracle_loss(st, wm, sch, samples)) / (wp[k] - wm[k])
+            print(f"h_rel {hr:g} w[{k}]: {g[k]:.10e} ({time.time() - t0:.0f} s)", flush=True)
+        grads[f"{hr:g}"] = [g.get(k) for k in range(8)]
     out = {"config": "3 nested boxes 97x97x49, 50 main steps, div B every %d (errlim %g), 200 line samples"
-                     % (st.params.divb_every, st.params.divb_errlim), "components": comps,
-           "u": u0.tolist(), "h_rel": 1e-4, "h": (1e-4 * scale).tolist(), "loss_fp64": L0,
-           "grad_u_fd_fp64": fd, "schedule": sch}
+                     % (st.params.divb_every, st.params.divb_errlim),
+           "wind": w0.tolist(), "loss_fp64": L0, "grad_wind_fd_fp64": grads, "schedule": sch}
     with open(os.path.join(HERE, name), "w") as fh:
         json.dump(out, fh, indent=1)
     print("written")

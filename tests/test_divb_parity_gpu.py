@@ -34,4 +34,9 @@ def test_divb_cadence_against_fp64(grid, steps):
     for n, rows in res.items():
         eg = np.array([r[1] for r in rows])
         er = np.array([r[2] for r in rows])
+        ratio = eg / np.maximum(er, 1e-30)
+        w = int(np.argmax(ratio))
+        bs = " ".join(f"{r[0]} {r[1]:.2e}/{r[2]:.2e}" for r in rows[31:34])
+        print(f"{grid} after {n}: median {np.median(eg):.2e} (ref32 {np.median(er):.2e}), largest ratio "
+              f"{ratio[w]:.2f} ({rows[w][0]} {eg[w]:.2e}/{er[w]:.2e}); {bs}")
         assert np.median(eg) <= 1.1 * np.median(er) + D.FLOOR, (n, np.median(eg), np.median(er))
