@@ -486,11 +486,15 @@ def roofline_from(rows):
 
 def _reference_steps(nsteps, warmup):
     """Time `nsteps` main steps of the nested grid on the CPU after `warmup`
-    untimed ones: the reference's own main loop where its translated build
-    exists ("reference"), else the oracle's restatement ("port"); both with
-    OpenMP on every host thread, no div B pass.  Returns (cell-updates/s,
-    seconds per step, kind, threads)."""
+    untimed ones, then one div B pass, charged at the GPU arm's cadence
+    (one pass per `divb_every` main steps, as the timed GPU steps hold):
+    the reference's own main loop and its own div B routines where its
+    translated build exists ("reference"), else the oracle's restatement
+    ("port"); the steps with OpenMP on every host thread, the pass as the
+    reference runs it (serial).  Returns (cell-updates/s, seconds per step
+    with the pass's share, kind, threads, seconds of the pass)."""
     from g3m3_gb300.state import make_config
+    every = make_config("nested").params.divb_every
     st = make_config("nested", divb_every=0)
     p = st.params
     cells = p.nx * p.ny * p.nz
@@ -512,7 +516,9 @@ def _reference_steps(nsteps, warmup):
             rm.steps(1)
             cu += sum(rm.box_steps()) * cells
         dt = time.perf_counter() - t0
-        return cu / dt, dt / nsteps, "reference", threads
+        pass_s = rm.divb_pass(p)
+        dt += pass_s * nsteps / every
+        return cu / dt, dt / nsteps, "reference", threads, pass_s
     from oracle.oracle import OracleModel
     om = OracleModel(st, omp=True)
     om.init_steps()
@@ -522,18 +528,23 @@ def _reference_steps(nsteps, warmup):
     for _ in range(nsteps):
         om.main_step()
     dt = time.perf_counter() - t0
-    return (om.cell_updates - cu0) / dt, dt / nsteps, "port", threads
+    t1 = time.perf_counter()
+    om.divb_all()
+    pass_s = time.perf_counter() - t1
+    dt += pass_s * nsteps / every
+    return (om.cell_updates - cu0) / dt, dt / nsteps, "port", threads, pass_s
 
 
 def cpu_baseline():
     """The reference's CPU path on a bounded sample: one main step of the
     same nested grid (about 27.7 M cell-updates) after one untimed step
     (the first touches the 1.9 GB of state)."""
-    v, sec, kind, threads = _reference_steps(1, 1)
+    v, sec, kind, threads, pass_s = _reference_steps(1, 1)
     what = ("the reference's main loop (translated Fortran, OpenMP)" if kind == "reference"
             else "the oracle's restatement (OpenMP)")
     return {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": kind,
-            "sample": f"1 main step of the nested 5-box grid after 1 untimed (no divB), {what}, {sec:.1f} s"}
+            "sample": f"1 main step of the nested 5-box grid after 1 untimed, {what}, plus one div B pass "
+                      f"({pass_s:.1f} s, charged as 1/10 per main step, the GPU arm's cadence): {sec:.1f} s per step"}
 
 
 # ------------------------------------------------------------ reference arm
@@ -544,20 +555,42 @@ def run_reference(args):
     from g3m3_gb300.state import make_config
     st = make_config("nested", divb_every=0)
     steps, warmup = min(args.steps, 2), min(args.warmup, 1)
-    v, sec, kind, threads = _reference_steps(steps, warmup)
+    v, sec, kind, threads, pass_s = _reference_steps(steps, warmup)
     what = ("the reference's main loop (its Fortran translated to C, OpenMP loops with private temporaries)"
             if kind == "reference" else "the oracle's restatement of the reference (OpenMP)")
-    sample = f"{steps} main step(s) of the nested 5-box grid after {warmup} warm-up (no divB), {what}"
+    sample = (f"{steps} main step(s) of the nested 5-box grid after {warmup} warm-up, {what}, plus one div B "
+              f"pass of the reference's own routines ({pass_s:.1f} s, charged as 1/10 per main step: the GPU "
+              f"arm's div B cadence, so both arms run the same work per step)")
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": "cell-updates/s", "n_gpus": ws,
             "steps": steps, "warmup": warmup, "ms_per_step": sec * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": {"workload": WORKLOAD, "boxes": st.params.n_grids,
                                             "box": [st.params.nx, st.params.ny, st.params.nz],
                                             "cells_per_box": st.params.nx * st.params.ny * st.params.nz,
+                                            "divb_every": make_config("nested").params.divb_every,
                                             "parallelism": f"host OpenMP, {threads} threads"},
             "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": kind,
                              "sample": sample},
             "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def run_adjoint_profile():
+    """The small case of the adjoint's ncu captures: 10 main steps of 3
+    nested 65x65x33 boxes (a 2.6 GB tape), checkpoints every 2, 50
+    samples; one forward, one backward."""
+    from g3m3_gb300.adjoint import MisfitRun, line_samples, wind_of
+    from g3m3_gb300.api import Context, Model
+    from g3m3_gb300.state import make_config
+    st = make_config("nested", limit=32, n_grids=3)
+    with Context(0) as ctx:
+        m = Model(ctx, st)
+        run = MisfitRun(m, st, 10, line_samples(st, 10, n=50), checkpoint_every=2)
+        loss = run.loss(wind_of(st.params))
+        run.adj.backward(state=False)
+        print(json.dumps({"adjoint_profile_case": "3 nested boxes 65x65x33, 10 main steps, checkpoints every 2",
+                          "loss": loss, "backward_phases_s": run.adj.phases()[:3]}))
+        run.adj.close()
+        m.close()
 
 
 def run_profile(args):
@@ -571,11 +604,13 @@ def run_profile(args):
     with Context(0) as ctx:
         m = Model(ctx, st)
         variant = m.autotune()   # 24 flux-correction launches, as in the benchmark
+        if args.contracted:
+            m.ctx.check(m.L.g3m3_model_set_contracted(m.h, 1))
         m.init_steps()
         m.run(args.warmup + args.steps, graph=False)
         k, _ = m.stats()
         print(json.dumps({"profile_case": f"{args.profile_boxes} box(es) 121x121x61", "main_steps": args.warmup + args.steps,
-                          "kernel_launches": k, "fcsmooth_variant": variant}))
+                          "kernel_launches": k, "fcsmooth_variant": variant, "contracted": bool(args.contracted)}))
 
 
 def main():
@@ -590,11 +625,18 @@ def main():
     ap.add_argument("--adjoint-only", action="store_true", help="run only the adjoint leg and print its block")
     ap.add_argument("--profile", action="store_true",
                     help="profiling case for ncu: one 121x121x61 box, warmup+steps main steps, host-loop launches")
+    ap.add_argument("--adjoint-profile", action="store_true",
+                    help="profiling case for ncu: the adjoint of 10 main steps on 3 nested 65x65x33 boxes, "
+                         "checkpoints every 2, one forward and one backward")
+    ap.add_argument("--contracted", action="store_true",
+                    help="with --profile: the contracted flavour of push_ion")
     ap.add_argument("--profile-boxes", type=int, default=1,
                     help="nested 121x121x61 boxes of the profiling case (2: flanks and corer run too)")
     args = ap.parse_args()
     if args.profile:
         return run_profile(args)
+    if args.adjoint_profile:
+        return run_adjoint_profile()
     if args.adjoint_only:
         print(json.dumps({"adjoint": run_adjoint(0)}), flush=True)
         return None

@@ -116,6 +116,39 @@ class RefMain:
         self.lib.ref_main_steps(ctypes.addressof(k))
         self._check()
 
+    def divb_pass(self, p):
+        """One div B cleaning pass as the main loop makes it at a fluid-file
+        time (3d_main.f90:3363-3408): divB_correct twice per box from the
+        outermost in, flanks_synced of bx, by, bz from box n_grids-1 down,
+        bndry_corer from box 1 up, each the reference's own routine called
+        on the loop's arrays.  Returns the seconds it took."""
+        import time
+        nx, ny, nz, ng = p.nx, p.ny, p.nz, p.n_grids
+        i32 = lambda v: ctypes.byref(ctypes.c_int32(v))
+        pos = np.array([nx * ny, nx, 1, 0, -1, -nx, -nx * ny], np.int32)
+        xs = np.ascontiguousarray(self.array("xspac"), np.float32)
+        err = ctypes.c_float(p.divb_errlim)
+        gmin, gmax = self.array("grid_minvals"), self.array("grid_maxvals")
+        grids = [np.ascontiguousarray(a[:, q]) for q in range(3) for a in (gmin, gmax)]
+        gptr = [g.ctypes.data_as(ctypes.c_void_p) for g in grids]
+        b = [self.array(n).ctypes.data_as(ctypes.c_void_p) for n in ("bx", "by", "bz")]
+        corer = [a["name"] for a in self.meta["subroutines"]["bndry_corer"]["args"]]
+        fields = [self.array(n).ctypes.data_as(ctypes.c_void_p) for n in corer[:34]]
+        t0 = time.perf_counter()
+        for box in range(ng, 0, -1):
+            for _ in range(2):
+                self.lib.ref_divb_correct(i32(nx), i32(ny), i32(nz), i32(ng), i32(box), i32(7),
+                                          pos.ctypes.data_as(ctypes.c_void_p), xs.ctypes.data_as(ctypes.c_void_p),
+                                          ctypes.byref(err), *b)
+        for box in range(ng - 1, 0, -1):
+            for q in range(3):
+                self.lib.ref_flanks_synced(b[q], i32(nx), i32(ny), i32(nz), i32(ng), i32(box), *gptr)
+        for box in range(1, ng):
+            self.lib.ref_bndry_corer(*fields, i32(nx), i32(ny), i32(nz), i32(ng), i32(box), *gptr)
+        dt = time.perf_counter() - t0
+        self._check()
+        return dt
+
     def _check(self):
         if ctypes.c_int.in_dll(self.lib, "ref_main_stopped").value:
             raise RuntimeError("the reference's main loop executed STOP")
