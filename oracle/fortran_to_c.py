@@ -1711,9 +1711,12 @@ def compile_ref(out_dir=OUT, cc="gcc", stem="g3m3_ref"):
     cpath = os.path.join(out_dir, stem + ".c")
     so = os.path.join(out_dir, "lib" + stem + ".so")
     omp = ["-fopenmp"] if stem.endswith("_omp") else []
+    # the OpenMP builds time the reference's CPU path: -O3 (vectorised loops;
+    # the same bits, contraction and fast-math staying off)
+    opt = "-O3" if omp else "-O2"
     # warnings are not shown, but the ones that reveal a mistranslated
     # argument (a pointer where a value belongs, or the reverse) are errors
-    r = subprocess.run([cc] + omp + ["-O2", "-fPIC", "-shared", "-std=gnu11", "-ffp-contract=off",
+    r = subprocess.run([cc] + omp + [opt, "-fPIC", "-shared", "-std=gnu11", "-ffp-contract=off",
                         "-fno-fast-math", "-fwrapv", "-Werror=int-conversion",
                         "-Werror=incompatible-pointer-types", "-Werror=implicit-function-declaration",
                         "-Werror=pointer-to-int-cast", "-Werror=int-to-pointer-cast",
