@@ -60,7 +60,7 @@ FILES = [
     "sub_bndry_outer", "sub_bndry_inner", "sub_bndry_flanks", "sub_flanks",
     "sub_bndry_corer", "sub_corer", "sub_flanks_synced", "sub_divB_correct",
     "sub_sparse_solver", "sub_banded_tpose", "cft_trilin_interp",
-    "cft_findgrid", "sub_flux_counter",
+    "cft_findgrid", "sub_flux_counter", "sub_dipole", "sub_set_resist",
 ]
 
 
@@ -1436,6 +1436,8 @@ class Gen:
         loop_body = u.body
         u.body = u.init_body
         init_body = self.body(u)
+        u.body = u.fresh_body
+        fresh_body = self.body(u)
         u.body = loop_body
         for n in self.locals_used:
             u.sym(n)
@@ -1509,6 +1511,16 @@ class Gen:
         out.append("  if (setjmp(ref_jmp)) { ref_jmp_armed = 0; return; }")
         out.append("  ref_jmp_armed = 1;")
         out += init_body
+        out.append("  goto L_return;")
+        out.append("L_return:;")
+        out.append("  ref_jmp_armed = 0;")
+        out.append("}")
+        out.append(f"/* the fresh start (initial state), lines {u.fresh_lines[0]}-{u.fresh_lines[1]} */")
+        out.append("void ref_main_fresh_start(void) {")
+        out += prolog
+        out.append("  if (setjmp(ref_jmp)) { ref_jmp_armed = 0; return; }")
+        out.append("  ref_jmp_armed = 1;")
+        out += fresh_body
         out.append("  goto L_return;")
         out.append("L_return:;")
         out.append("  ref_jmp_armed = 0;")
@@ -1620,6 +1632,27 @@ def parse_main_loop(path, module_dir, overrides):
         raise TranslateError("no time-step set-up loop before the time loop")
     u.init_body = body[init[0]:init[1] + 1]
     u.init_lines = (body[init[0]][0], body[init[1]][0])
+    # the fresh start: the ELSE branch of the top-level "if(.not.start)"
+    # before the loop (the initial state, dipole, inner-boundary lists,
+    # resistivity)
+    u.fresh_body, u.fresh_lines = [], (0, 0)
+    for j in range(start):
+        if re.match(r"^if\s*\(\s*\.not\.\s*start\s*\)\s*then$", body[j][1]):
+            d, e_else = 0, None
+            for e in range(j, start):
+                st = body[e][1]
+                if re.match(r"^if\s*\(.*\)\s*then$", st):
+                    d += 1
+                elif re.match(r"^end\s*if$", st):
+                    d -= 1
+                    if d == 0:
+                        break
+                elif d == 1 and st == "else":
+                    e_else = e
+            if e_else is not None:
+                u.fresh_body = body[e_else + 1:e]
+                u.fresh_lines = (body[e_else + 1][0], body[e - 1][0])
+            break
     for mod in u.uses:
         parse_module_params(os.path.join(module_dir, f"mod_{mod}.f90"), u)
     for n, v in overrides.items():
@@ -1701,7 +1734,8 @@ def _translate_main(code_dir, tag, overrides, out_dir, omp, real8):
         fh.write("\n".join(src + main_src) + "\n")
     meta = g.meta(order)
     meta["main"] = {"variables": main_meta, "overrides": overrides, "openmp": omp,
-                    "loop_lines": list(prog.loop_lines), "init_lines": list(prog.init_lines)}
+                    "loop_lines": list(prog.loop_lines), "init_lines": list(prog.init_lines),
+                    "fresh_lines": list(prog.fresh_lines)}
     with open(os.path.join(out_dir, stem + ".json"), "w") as fh:
         json.dump(meta, fh, indent=1)
     return cpath

@@ -116,6 +116,53 @@ class RefMain:
         self.lib.ref_main_steps(ctypes.addressof(k))
         self._check()
 
+    def fresh_start(self, p, consts, capacity=None):
+        """The reference's fresh start (the ELSE branch of its
+        ``if(.not.start)``, 3d_main.f90:1194-1634: dipole field, corotating
+        ionospheric plasma, solar wind, speed clip, inner-boundary lists,
+        resistivity) for the grid and constants of `p`, with the derived
+        constants `consts` the reference computes before it (3d_main.f90:
+        790-880): r_inner, zero/mid/srf_bndry, erho, b0, cs_inner, alpha_e,
+        cs_wind, xdip; no rotation, tilt, moon or torus.  Returns the fields
+        (34, n_grids, nz, ny, nx), b0 (3, ...), the resistivity and the
+        inner-boundary lists as make_state's ``lists``."""
+        ng, mb = p.n_grids, p.mbndry
+        gmin, gmax = self.array("grid_minvals"), self.array("grid_maxvals")
+        for b in range(ng):
+            gmin[b] = [p.grd_xmin[b], p.grd_ymin[b], p.grd_zmin[b]]
+            gmax[b] = [p.grd_xmax[b], p.grd_ymax[b], p.grd_zmax[b]]
+        self.array("xspac")[...] = np.array(p.xspac[:ng], np.float32)
+        for k in ("rmassq", "rmassh", "rmasso", "gamma", "resist", "re_equiv", "srho", "rho_frac", "spress",
+                  "spx", "spy", "spz", "ti_te"):
+            self.set(**{k: float(getattr(p, k))})
+        for k in ("r_inner", "zero_bndry", "mid_bndry", "srf_bndry", "erho", "cs_inner", "alpha_e", "cs_wind"):
+            self.set(**{k: float(consts[k])})
+        self.set(t=0.0, utstart=0.0, t_equiv=1.0, tsave=BIG, tmax=BIG, deltg=BIG, deltinj=BIG, planet_per=1.0,
+                 moon_per=1.0, moon_init_rot=0.0, moon_orbit_rad=0.0)
+        self.set_common("rotation", v_rot=p.v_rot, r_rot=p.r_rot, xdip=consts["xdip"], ydip=0.0, zdip=0.0,
+                        sin_tilt=0.0, cos_tilt=1.0, b0=consts["b0"])
+        cap = capacity or p.nx * p.ny * p.nz
+        lists = {}
+        for key in ("srf", "mid", "zero"):
+            ij = np.zeros((cap, 3, mb), np.int32)
+            parm = np.zeros((cap, 7, mb), np.float32)
+            self.set_allocatable("ij" + key, ij, (mb, 3, cap))
+            self.set_allocatable("parm_" + key, parm, (mb, 7, cap))
+            self.set(**{"m" + key: cap})
+            lists[key] = (ij, parm)
+        self.lib.ref_main_fresh_start()
+        self._check()
+        out = {"fields": self.fields().copy(),
+               "b0": np.stack([self.array(f"b{c}0").copy() for c in "xyz"]),
+               "resistive": self.array("resistive").copy()}
+        for key, (ij, parm) in lists.items():
+            num = self.array("num" + key).copy()
+            m = int(num.max()) if num.size else 0
+            out["ij" + key] = ij[:max(m, 1)].copy()
+            out["parm_" + key] = parm[:max(m, 1)].copy()
+            out["num" + key] = num
+        return out
+
     def divb_pass(self, p):
         """One div B cleaning pass as the main loop makes it at a fluid-file
         time (3d_main.f90:3363-3408): divB_correct twice per box from the
