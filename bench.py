@@ -290,6 +290,7 @@ def run_ours(args):
         line["batched"] = run_batched(args, local)
     if not args.no_adjoint:
         line["adjoint"] = run_adjoint(local)
+        line["batched_adjoint"] = run_batched_adjoint(local)
     if not args.no_cpu and ws == 1:
         line["cpu_baseline"] = cpu_baseline()
     return line
@@ -429,6 +430,68 @@ def run_adjoint(device, nsteps=50, every=10, nsamp=200):
                                  "divb_reverse": phases[5]},
             "note": "forward: the engine's graph-replayed main steps; backward: per checkpoint interval the steps "
                     "re-run with snapshots, then the reverse kernels"}
+
+
+def run_batched_adjoint(device, members=8, nsteps=10, every=1, nsamp=200):
+    """BASELINE config 4: 8 ensemble members on nested grids of 5 boxes of
+    121x121x61 (upstream conditions from the seed), the forward of all
+    members as one CUDA graph per main step, then each member's adjoint of
+    the same 10 main steps (checkpoints every step: one step's tape, about
+    30 GB, is what one member's backward holds) for the misfit of its own
+    200 line samples; members' gradients one after another, sharing the
+    tape's memory.  adjoint_over_forward = the members' backward time /
+    the batched forward's, per main step."""
+    import torch
+    from g3m3_gb300.adjoint import ensemble_gradients, line_samples
+    from g3m3_gb300.api import Context, Ensemble
+    from g3m3_gb300.state import ensemble_member
+    ctx = Context(device)
+    states = [ensemble_member(i, limits=(60,)) for i in range(members)]
+    ens = Ensemble(ctx, states)
+    ens.autotune()
+    ens.init_steps()
+    stream = torch.cuda.ExternalStream(ens.stream)
+
+    def ev_time(fn, s=stream):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(s)
+        fn()
+        e1.record(s)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    ens.run(2, graph=True)                     # warm-up: graph captures
+    for m, st in zip(ens.members, states):
+        m.upload(st)
+    ens.init_steps()
+    cu0 = ens.stats()[2]
+    fwd_ms = ev_time(lambda: ens.run(nsteps, graph=True))
+    cu = ens.stats()[2] - cu0
+    # each member's gradient: CUDA events on that member's stream
+    recs = ensemble_gradients(ens, states, nsteps, lambda st: line_samples(st, nsteps, n=nsamp),
+                              checkpoint_every=every,
+                              timer=lambda m, fn: ev_time(fn, torch.cuda.ExternalStream(m.stream)))
+    p = states[0].params
+    ens.close()
+    ctx.close()
+    bwd_ms = sum(r["backward_ms"] for r in recs)
+    afwd_ms = sum(r["forward_ms"] for r in recs)
+    return {"workload": f"{members} ensemble members, nested grids of 5 boxes of 121x121x61 (upstream conditions "
+                        f"from the seed), {nsteps} main steps; forward: all members in one CUDA graph per main "
+                        f"step; gradient: each member's adjoint (checkpoints every {every} step(s), {nsamp} line "
+                        f"samples of its own), members one after another sharing the tape's memory",
+            "members": members, "box": [p.nx, p.ny, p.nz], "boxes": p.n_grids, "main_steps": nsteps,
+            "checkpoint_every": every,
+            "forward": {"value": cu / (fwd_ms / 1e3), "unit": "cell-updates/s", "ms_per_step": fwd_ms / nsteps},
+            "gradient": {"value": cu / ((afwd_ms + bwd_ms) / 1e3), "unit": "cell-updates/s (forward with "
+                         "checkpoints + backward, all members)", "ms_per_step": (afwd_ms + bwd_ms) / nsteps},
+            "adjoint_forward_ms_per_step": afwd_ms / nsteps, "backward_ms_per_step": bwd_ms / nsteps,
+            "adjoint_over_forward": bwd_ms / fwd_ms, "gradient_over_forward": (afwd_ms + bwd_ms) / fwd_ms,
+            "tape_bytes_per_member": max(r["tape_bytes"] for r in recs),
+            "losses": [r["loss"] for r in recs],
+            "grad_wind_norms": [float(np.linalg.norm(r["grad_wind"])) for r in recs]}
 
 
 KERNELS = {  # id: (name, launches per box-step)

@@ -219,6 +219,39 @@ class MisfitRun:
         return val
 
 
+def ensemble_gradients(ensemble, states, nsteps, samples_of, checkpoint_every=1, cg_errlim=0.0, timer=None):
+    """Batched + adjoint: every member of an ``Ensemble`` with its own
+    virtual-spacecraft misfit and its gradient.  The members' gradients are
+    taken one after another on their own models, each adjoint created,
+    run (forward with checkpoints, backward) and destroyed before the next,
+    so the members share the memory of one tape (one checkpoint interval
+    of a 5-box 121x121x61 member is about 30 GB per main step).  Returns
+    one dict per member: loss, dL/d(wind parameters), tape bytes, the
+    backward's phases, and, with ``timer`` (timer(model, fn) runs fn and
+    returns its milliseconds on the model's stream), the forward's and
+    backward's times."""
+    out = []
+    for m, st in zip(ensemble.members, states):
+        run = MisfitRun(m, st, nsteps, samples_of(st), checkpoint_every, cg_errlim)
+        w = wind_of(st.params)
+        rec = {}
+        if timer is None:
+            rec["loss"] = run.loss(w)
+            g = run.adj.backward(state=False)
+        else:
+            box = {}
+            rec["forward_ms"] = timer(m, lambda: box.setdefault("loss", run.loss(w)))
+            rec["loss"] = box["loss"]
+            rec["backward_ms"] = timer(m, lambda: box.setdefault("g", run.adj.backward(state=False)))
+            g = box["g"]
+        rec["grad_wind"] = g["params"]
+        rec["tape_bytes"] = run.adj.tape_bytes()
+        rec["phases_s"] = run.adj.phases()[:3]
+        run.adj.close()
+        out.append(rec)
+    return out
+
+
 def _function():
     import torch
 

@@ -179,3 +179,29 @@ def test_config3_gradient():
         print("  fd     ", fd)
     assert max(errs["1e-05"]) <= GRAD_TOL, errs
     assert max(errs["0.0001"]) <= 1e-2, errs
+
+
+def test_ensemble_gradients_match_single_members():
+    """Batched + adjoint (g3m3_gb300.adjoint.ensemble_gradients): each
+    member's misfit, taken on the ensemble's member model, equals the one a
+    standalone model of the same state gives bit for bit, and its gradient
+    to 1e-6 relative (the reverse kernels add with atomics, whose order of
+    summation varies from run to run)."""
+    from g3m3_gb300.adjoint import MisfitRun, ensemble_gradients, line_samples, wind_of
+    from g3m3_gb300.api import Context, Ensemble, Model
+    from g3m3_gb300.state import ensemble_member
+    states = [ensemble_member(i, limits=(8,), n_grids=3, divb_every=2, divb_errlim=1e-6) for i in range(2)]
+    samples_of = lambda st: line_samples(st, 3, n=30)
+    with Context() as ctx:
+        ens = Ensemble(ctx, states)
+        got = ensemble_gradients(ens, states, 3, samples_of, checkpoint_every=1)
+        ens.close()
+    for st, g in zip(states, got):
+        with Context() as ctx:
+            m = Model(ctx, st)
+            run = MisfitRun(m, st, 3, samples_of(st), checkpoint_every=1)
+            loss = run.loss(wind_of(st.params))
+            want = run.adj.backward(state=False)["params"]
+        assert loss == g["loss"]
+        assert np.allclose(g["grad_wind"], want, rtol=1e-6, atol=1e-9 * np.abs(want).max()), (want, g["grad_wind"])
+        assert np.abs(want).max() > 0
