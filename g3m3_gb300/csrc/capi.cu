@@ -647,13 +647,9 @@ int g3m3_bande(g3m3_ctx* ctx, float* efldx, float* efldy, float* efldz, const fl
     int nm[G3M3_MAX_GRIDS * 4], nzr[G3M3_MAX_GRIDS * 4];
     if (mbndry > (int)(sizeof nm / sizeof nm[0])) return set_err(ctx, G3M3_ERR_ARG, "mbndry too large");
     // the counts are host integers in the reference; read them on the host
-    if (is_device_ptr(nummid) || is_device_ptr(numzero)) {
-      G3M3_CUDA(ctx, cudaMemcpy(nm, nummid, mbndry * sizeof(int), cudaMemcpyDeviceToHost));
-      G3M3_CUDA(ctx, cudaMemcpy(nzr, numzero, mbndry * sizeof(int), cudaMemcpyDeviceToHost));
-    } else {
-      std::memcpy(nm, nummid, mbndry * sizeof(int));
-      std::memcpy(nzr, numzero, mbndry * sizeof(int));
-    }
+    // (device arrays on the context's stream, after the work queued on it)
+    int st;
+    if ((st = host_ints(ctx, nummid, mbndry, nm)) || (st = host_ints(ctx, numzero, mbndry, nzr))) return st;
     BandEListArgs l{};
     for (int q = 0; q < 3; q++) {
       l.efld[q] = a.efld[q];
@@ -939,8 +935,8 @@ int g3m3_bndry_inner(g3m3_ctx* ctx, float* const f[G3M3_NFIELDS], const float* p
   const int* cp[3] = {numsrf, nummid, numzero};
   for (int q = 0; q < 3; q++) {
     if (mb > G3M3_MAX_GRIDS) return set_err(ctx, G3M3_ERR_ARG, "mbndry too large");
-    if (is_device_ptr(cp[q])) G3M3_CUDA(ctx, cudaMemcpy(cnt[q], cp[q], mb * sizeof(int), cudaMemcpyDeviceToHost));
-    else std::memcpy(cnt[q], cp[q], mb * sizeof(int));
+    const int st = host_ints(ctx, cp[q], mb, cnt[q]);
+    if (st) return st;
   }
   const int caps[3] = {msrf, mmid, mzero};
   for (int q = 0; q < 3; q++) {
