@@ -365,7 +365,7 @@ ADJOINT_WORKLOAD = ("adjoint of 50 main steps on 3 nested boxes of 97x97x49 (2x 
 
 
 def run_adjoint(device, nsteps=50, every=10, nsamp=200):
-    """BASELINE config 3: the adjoint of 50 main steps of 3 nested 97x97x49
+    """The adjoint of 50 main steps of 3 nested 97x97x49
     boxes, checkpointed every 10 steps.  Times (CUDA events on the model's
     stream): the plain forward (the engine's step, graph-replayed), the
     adjoint's forward (host-launched, with checkpoints and the misfit), and
@@ -433,7 +433,7 @@ def run_adjoint(device, nsteps=50, every=10, nsamp=200):
 
 
 def run_batched_adjoint(device, members=8, nsteps=10, every=1, nsamp=200):
-    """BASELINE config 4: 8 ensemble members on nested grids of 5 boxes of
+    """Batched + adjoint: 8 ensemble members on nested grids of 5 boxes of
     121x121x61 (upstream conditions from the seed), the forward of all
     members as one CUDA graph per main step, then each member's adjoint of
     the same 10 main steps (checkpoints every step: one step's tape, about
@@ -684,7 +684,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the 16-member ensemble leg")
-    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg (BASELINE config 3)")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint legs (3 x 97x97x49 boxes; 8 members of 5 x 121x121x61)")
     ap.add_argument("--adjoint-only", action="store_true", help="run only the adjoint leg and print its block")
     ap.add_argument("--profile", action="store_true",
                     help="profiling case for ncu: one 121x121x61 box, warmup+steps main steps, host-loop launches")

@@ -1,5 +1,5 @@
-"""FP64 central differences of the virtual-spacecraft misfit of BASELINE
-config 3 (TEST INFRASTRUCTURE): 50 main steps of 3 nested boxes of
+"""FP64 central differences of the virtual-spacecraft misfit of the adjoint
+benchmark (TEST INFRASTRUCTURE): 50 main steps of 3 nested boxes of
 97x97x49, div B every 10 steps, 200 samples along the seeded line of
 g3m3_gb300.adjoint.line_samples.  The time-step schedule is the oracle's
 FP32 run's (the reference's FP32 bits); the misfit is evaluated with the
@@ -12,12 +12,12 @@ step is exact.  h_k = h_rel * scale_k, scale_k the magnitude of the
 parameter's group (srho; |sp|; spress; |sb|).  The gradient with respect
 to the upstream conditions u = (n, v, B) follows by the chain rule through
 the exact Jacobian of g3m3_gb300.adjoint.upstream_wind.  Two steps are
-taken: h_rel = 1e-4 (BASELINE config 3's) and 1e-5; the misfit has kinks
+taken: h_rel = 1e-4 (the benchmark's stated step) and 1e-5; the misfit has kinks
 (limiter and guard branches), and the difference quotients of the two
 steps differ by more than the smaller one differs from the adjoint.
 
-Writes adjoint_fd_config3.json beside this file; the GPU test
-tests/test_adjoint_gpu.py::test_config3_gradient compares the library's
+Writes adjoint_fd_3x97x97x49.json beside this file; the GPU test
+tests/test_adjoint_gpu.py::test_nested_97_gradient compares the library's
 adjoint with it.
 
     python tests/golden/make_adjoint_fd.py [--params 0,1,..] [--hrel 1e-4,1e-5]
@@ -39,7 +39,7 @@ import _adjoint_ref as R  # noqa: E402
 NSTEPS = 50
 
 
-def config3(**over):
+def adjoint_grid(**over):
     from g3m3_gb300.state import make_config
     return make_config("nested", limit=48, n_grids=3, **over)
 
@@ -65,10 +65,10 @@ def main(argv=()):
         over["divb_errlim"] = float(opts["--errlim"])
     comps = [int(x) for x in opts["--params"].split(",")] if "--params" in opts else list(range(8))
     hrels = [float(x) for x in opts["--hrel"].split(",")] if "--hrel" in opts else [1e-4, 1e-5]
-    name = opts.get("--out", "adjoint_fd_config3.json")
+    name = opts.get("--out", "adjoint_fd_3x97x97x49.json")
     from g3m3_gb300.adjoint import line_samples, wind_of
     from oracle.oracle import OracleModel
-    st = config3(**over)
+    st = adjoint_grid(**over)
     samples = line_samples(st, NSTEPS, n=200)
     om = OracleModel(st, omp=True)
     om.init_steps()

@@ -127,11 +127,11 @@ def test_torch_function_upstream_gradient():
     assert np.allclose(u.grad.numpy(), J.T @ gw, rtol=1e-6, atol=1e-12 * np.abs(J.T @ gw).max())
 
 
-def test_config3_gradient():
-    """BASELINE config 3: the adjoint of 50 main steps of three nested
+def test_nested_97_gradient():
+    """The adjoint of 50 main steps of three nested
     97x97x49 boxes (div B every 10 steps), checkpointed every 10 steps,
     200 samples, against FP64 central differences of the same run under the
-    same time-step schedule (tests/golden/adjoint_fd_config3.json, made by
+    same time-step schedule (tests/golden/adjoint_fd_3x97x97x49.json, made by
     tests/golden/make_adjoint_fd.py), in the eight wind-face parameters and,
     through the exact Jacobian of upstream_wind, in u = (n, v, IMF).
 
@@ -146,7 +146,7 @@ def test_config3_gradient():
     from g3m3_gb300.adjoint import MisfitRun, line_samples, wind_of, wind_scales
     from g3m3_gb300.api import Context, Model
     from g3m3_gb300.state import CONFIGS, Setup, make_config
-    fx = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "adjoint_fd_config3.json")))
+    fx = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "adjoint_fd_3x97x97x49.json")))
     st = make_config("nested", limit=48, n_grids=3)
     setup = Setup(**dict(CONFIGS["nested"], limit=48, n_grids=3))
     w = wind_of(st.params)

@@ -1,16 +1,16 @@
 """div B at the benchmark configurations' cadence, against the FP64 build.
 
-BASELINE config 0 (one 61x61x31 box, div B every 5 main steps, errlim 1e-6)
-for 20 main steps and config 1 (the production nested grid of five
-121x121x61 boxes, div B every 10, errlim 1e-4) for 20 main steps: the
+The one-box grid (61x61x31, div B every 5 main steps, errlim 1e-6)
+for 20 main steps and the production nested grid (five 121x121x61
+boxes, div B every 10, errlim 1e-4) for 20 main steps: the
 library's step engine, the oracle's FP32 main loop (the reference's FP32
 bits, FP32 dot products in the CG) and the oracle's FP64 build run from the
 same seeded state.  Right after the first pass the 31 fields div B does not
 touch are still the reference's bits; at every checkpoint every field of
 the library is at most SLACK times as far from the FP64 run as the
 reference's FP32 build is, plus FLOOR (tests/_divb_parity.py).  Measured
-(GB300): the ratio of the two distances is at most 1.09 on config 0 and
-2.23 on config 1 (opresx after 20 steps, 2.5e-7 against 1.5e-7); medians
+(GB300): the ratio of the two distances is at most 1.09 on the one-box grid and
+2.23 on the nested grid (opresx after 20 steps, 2.5e-7 against 1.5e-7); medians
 over the 34 fields agree to 5 %.
 """
 import numpy as np

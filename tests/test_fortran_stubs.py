@@ -67,8 +67,9 @@ def test_every_header_function_and_routine_is_covered():
 
 
 def _reference_code():
-    base = os.environ.get("G3M3_REFERENCE", "/root/reference")
-    code = os.path.join(base, "code")
+    sys.path.insert(0, ROOT)
+    import __graft_entry__
+    code = os.path.join(__graft_entry__.REFERENCE, "code")
     return code if os.path.isdir(code) else None
 
 
