@@ -87,10 +87,14 @@ struct Off7 {
 
 // ------------------------------------------------------------------ push_ion
 // 168 registers (three blocks of 128 per SM; a small spill) timed fastest
-// against the unbounded 255, 128 and 80; a form that sums the stencil
-// contributions of a tile in a shared-memory ring with shared atomics before
-// adding them to global memory was slower (289 against 226 us per launch on
-// a 97x97x49 box, both with IEEE division) and is not kept.
+// against the unbounded 255, 128 and 80.  Also slower, per launch on a
+// 97x97x49 box: a form that sums the stencil contributions of a tile in a
+// shared-memory ring with shared atomics before adding them to global
+// memory (289 against 226 us, both with IEEE division); a tile marching
+// along z with the 13 stencil fields of three planes staged in shared
+// memory (350 against 215 us: two barriers per plane); each thread's 108
+// inputs copied into its own shared-memory column by asynchronous copies
+// issued at once (238 against 215 us: the sweep still holds 168 registers).
 __global__ void __launch_bounds__(128, 3) k_adj_push_ion(const __grid_constant__ AdjPushIonArgs a) {
   const Dims d = a.d;
   const Cell3 p = cell3(d);
