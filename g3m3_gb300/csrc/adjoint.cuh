@@ -3,10 +3,13 @@
 //
 // Conventions.  For every forward array there is an adjoint array of the
 // same shape ("a_" prefix).  A reverse kernel reads the adjoint of what its
-// forward kernel wrote, adds J^T of it into the adjoints of what the forward
-// kernel read (atomically: several cells read one input), and clears the
-// adjoint of every value the forward kernel overwrote.  Primal values come
-// from the tape's snapshots or are recomputed from them.
+// forward kernel wrote and adds J^T of it into the adjoints of what the
+// forward kernel read: by atomic additions where several cells read one
+// input, or as a gather, each input's thread summing the shares it receives
+// (the Lapidus and flux-correction reverses).  The adjoint of every value
+// the forward kernel overwrote is cleared, by the kernel or, after a
+// gather that others still read, by its caller.  Primal values come from
+// the tape's snapshots or are recomputed from them.
 #pragma once
 
 #include "bndry.cuh"

@@ -6,7 +6,9 @@
 // adjoints of the forward kernel's inputs.  A cell's stencil inputs are
 // shared with its neighbours, so those additions are atomic (fire-and-
 // forget reductions in L2; the order of the FP32 sums is not fixed, which
-// changes gradients by rounding only).  The per-cell arithmetic of the
+// changes gradients by rounding only), except in the Lapidus and
+// flux-correction reverses, which gather each input's shares in the
+// input's own thread.  The per-cell arithmetic of the
 // pushes, fields, Lapidus and flux-correction kernels comes from the
 // reverse sweeps in adj_cells.cuh; the boundary, nested-grid, guard and
 // div B reverses are written out here.
