@@ -11,6 +11,12 @@
 
 #include "g3m3_oracle.h"
 
+/* The wind-face parameters as bndry_outer reads them: the identity, except
+ * in the forward-mode build (dual.h), which attaches their tangents. */
+#ifndef ORACLE_WIND
+#define ORACLE_WIND(k, v) (v)
+#endif
+
 #define IX(i, j, k) \
   ((size_t)((i) - 1) + (size_t)nx * ((size_t)((j) - 1) + (size_t)ny * (size_t)((k) - 1)))
 
@@ -62,24 +68,24 @@ void oracle_bndry_outer(float* const F[G3M3_NFIELDS],
     for (int j = 1; j <= ny; j++) {
       const size_t c = IX(1, j, k);
       float* q = f[0]; (void)q;
-      f[0][c] = p->srho; f[1][c] = p->spx; f[2][c] = p->spy; f[3][c] = p->spz;
-      f[4][c] = 0.5f * p->spress; f[5][c] = f[4][c]; f[6][c] = f[4][c];
-      f[10][c] = p->srho * p->rho_frac * frac_h;
-      f[11][c] = p->spx * p->rho_frac * frac_h;
-      f[12][c] = p->spy * p->rho_frac * frac_h;
-      f[13][c] = p->spz * p->rho_frac * frac_h;
-      f[14][c] = 0.5f * p->spress * p->rho_frac; f[15][c] = f[14][c]; f[16][c] = f[14][c];
-      f[20][c] = p->srho * ofrac * frac_o;
-      f[21][c] = p->spx * ofrac * frac_o;
-      f[22][c] = p->spy * ofrac * frac_o;
-      f[23][c] = p->spz * ofrac * frac_o;
-      f[24][c] = 0.5f * p->spress * ofrac; f[25][c] = f[24][c]; f[26][c] = f[24][c];
+      f[0][c] = ORACLE_WIND(0, p->srho); f[1][c] = ORACLE_WIND(1, p->spx); f[2][c] = ORACLE_WIND(2, p->spy); f[3][c] = ORACLE_WIND(3, p->spz);
+      f[4][c] = 0.5f * ORACLE_WIND(4, p->spress); f[5][c] = f[4][c]; f[6][c] = f[4][c];
+      f[10][c] = ORACLE_WIND(0, p->srho) * p->rho_frac * frac_h;
+      f[11][c] = ORACLE_WIND(1, p->spx) * p->rho_frac * frac_h;
+      f[12][c] = ORACLE_WIND(2, p->spy) * p->rho_frac * frac_h;
+      f[13][c] = ORACLE_WIND(3, p->spz) * p->rho_frac * frac_h;
+      f[14][c] = 0.5f * ORACLE_WIND(4, p->spress) * p->rho_frac; f[15][c] = f[14][c]; f[16][c] = f[14][c];
+      f[20][c] = ORACLE_WIND(0, p->srho) * ofrac * frac_o;
+      f[21][c] = ORACLE_WIND(1, p->spx) * ofrac * frac_o;
+      f[22][c] = ORACLE_WIND(2, p->spy) * ofrac * frac_o;
+      f[23][c] = ORACLE_WIND(3, p->spz) * ofrac * frac_o;
+      f[24][c] = 0.5f * ORACLE_WIND(4, p->spress) * ofrac; f[25][c] = f[24][c]; f[26][c] = f[24][c];
       f[G3M3_F_EPRES][c] = f[4][c] / p->ti_te;
       for (int s = 0; s < 3; s++)
         for (int o = 7; o <= 9; o++) f[10 * s + o][c] = 0.0f;
-      f[G3M3_F_BX][c] = p->sbx_wind - b0[0][c];
-      f[G3M3_F_BY][c] = p->sby_wind - b0[1][c];
-      f[G3M3_F_BZ][c] = p->sbz_wind - b0[2][c];
+      f[G3M3_F_BX][c] = ORACLE_WIND(5, p->sbx_wind) - b0[0][c];
+      f[G3M3_F_BY][c] = ORACLE_WIND(6, p->sby_wind) - b0[1][c];
+      f[G3M3_F_BZ][c] = ORACLE_WIND(7, p->sbz_wind) - b0[2][c];
     }
   for (int q = 0; q < G3M3_NFIELDS; q++) {
     float* a = f[q];

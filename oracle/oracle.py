@@ -62,14 +62,22 @@ class OracleState(ctypes.Structure):
 _LIBS = {}
 
 
-def lib(omp: bool = False, real8: bool = False):
-    name = "liboracle" + ("_r8" if real8 else "") + ("_omp" if omp else "") + ".so"
+def _dptr(a):
+    """A complex128 array (value, tangent) passed where the forward-mode
+    build's dual REAL pointers go."""
+    assert a.dtype == np.complex128 and a.flags["C_CONTIGUOUS"], (a.dtype, a.flags)
+    return ctypes.cast(a.ctypes.data, _fp)
+
+
+def lib(omp: bool = False, real8: bool = False, dual: bool = False):
+    name = ("liboracle_dual_omp" if dual else
+            "liboracle" + ("_r8" if real8 else "") + ("_omp" if omp else "")) + ".so"
     if name not in _LIBS:
         path = os.path.join(HERE, name)
         if not os.path.exists(path):
             build()
         L = ctypes.CDLL(path)
-        if real8:   # only the main-step entries (below) are used; their arguments are pointers
+        if real8 or dual:   # only the main-step entries (below) are used; their arguments are pointers
             _LIBS[name] = L
             return L
         from g3m3_gb300 import _lib as glib
@@ -85,26 +93,31 @@ class OracleModel:
     """Holds a full multi-box state in numpy arrays and steps it on the CPU
     with the oracle's restatement of the reference main loop.  With
     ``real8``, the FP64 build (every REAL in double precision, real8.h):
-    the state is float64, started from the FP32 state's values."""
+    the state is float64, started from the FP32 state's values.  With
+    ``dual``, the FP64 build in forward-mode dual numbers (dual.h): the
+    state is complex128, value in the real part and tangent in the
+    imaginary part (zero to start), and ``wind_tangent`` (8) seeds the
+    wind-face parameters' tangents."""
 
-    def __init__(self, state, omp: bool = False, real8: bool = False):
-        self.L = lib(omp, real8)
-        self.real8 = real8
+    def __init__(self, state, omp: bool = False, real8: bool = False, dual: bool = False):
+        self.L = lib(omp, real8, dual)
+        self.real8 = real8 or dual
+        self.dual = dual
         self.p = state.params
         p = self.p
-        ft = np.float64 if real8 else np.float32
+        ft = np.complex128 if dual else (np.float64 if real8 else np.float32)
         self.cur = state.cur.astype(ft)
         self.old = np.zeros_like(self.cur)
         self.wrk = self.cur.copy()   # wrkepres is read before it is written
         self.b0 = state.b0.astype(ft)
         self.resistive = state.resistive.astype(ft)
         self.lists = {k: np.ascontiguousarray(v) for k, v in state.lists.items()}
-        if real8:
+        if real8 or dual:
             for k in ("parm_srf", "parm_mid", "parm_zero"):
-                self.lists[k] = np.ascontiguousarray(self.lists[k], np.float64)
+                self.lists[k] = np.ascontiguousarray(self.lists[k], ft)
         box = (p.nz, p.ny, p.nx)
         self.scr = np.zeros((19,) + box, ft)
-        fptr = _rptr if real8 else globals()["fptr"]
+        fptr = _dptr if dual else (_rptr if real8 else globals()["fptr"])
         s = OracleState()
         for q in range(NFIELDS):
             s.cur[q] = fptr(self.cur[q]); s.old[q] = fptr(self.old[q]); s.wrk[q] = fptr(self.wrk[q])
@@ -126,6 +139,13 @@ class OracleModel:
                 getattr(s, n)[k] = fptr(self.scr[i])
             idx[n] = k + 1
         self.s = s
+
+    def set_wind_tangent(self, t):
+        """The tangents of the eight wind-face parameters (forward-mode build)."""
+        assert self.dual
+        arr = (ctypes.c_double * 8).in_dll(self.L, "oracle_wind_tangent")
+        for k in range(8):
+            arr[k] = float(t[k])
 
     def init_steps(self):
         self.L.oracle_init_steps(ctypes.byref(self.p), ctypes.byref(self.s))

@@ -51,6 +51,43 @@ def oracle_loss(state, wind, schedule, samples, delta=None, real8=True):
     return loss
 
 
+def oracle_jvp(state, wind, schedule, samples, wind_tangent=None, state_tangent=None):
+    """The misfit and its exact directional derivative along (wind_tangent,
+    state_tangent) from the oracle's FP64 build run in forward-mode dual
+    numbers (oracle/dual.h) under ``schedule``: the state tangent is added
+    after init_steps, where the library's state gradient is taken.  Returns
+    (loss, dloss)."""
+    import ctypes
+    from oracle.oracle import OracleModel
+    st = state.copy()
+    p = type(state.params)()
+    ctypes.memmove(ctypes.addressof(p), ctypes.addressof(state.params), ctypes.sizeof(p))
+    st.params = p
+    for k, v in zip(WIND, wind):
+        setattr(p, k, float(np.float32(v)))
+    om = OracleModel(st, omp=True, dual=True)
+    om.set_wind_tangent(np.zeros(8) if wind_tangent is None else wind_tangent)
+    om.init_steps()
+    if state_tangent is not None:
+        om.cur.imag[...] += state_tangent
+    xyz, step, target = samples
+    loss = dloss = 0.0
+    for s in range(len(schedule)):
+        for b in range(p.n_grids):
+            om.s.t_stepnew[b] = float(schedule[s][b])
+        assert om.main_step() == 0
+        sel = np.nonzero(np.asarray(step) == s + 1)[0]
+        if len(sel):
+            x = np.asarray(xyz)[sel]
+            v = sample_values(p, om.cur.real, x)
+            dv = sample_values(p, om.cur.imag, x)
+            r = v - np.asarray(target, np.float64)[sel]
+            ok = ~np.isnan(r)
+            loss += float((r[ok] ** 2).sum())
+            dloss += float((2.0 * r[ok] * dv[ok]).sum())
+    return loss, dloss
+
+
 def line_samples(state, nsteps, n=200, seed=20261205, scale=0.1):
     from g3m3_gb300.adjoint import line_samples as ls
     return ls(state, nsteps, n, seed, scale)

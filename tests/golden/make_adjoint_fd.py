@@ -16,12 +16,18 @@ taken: h_rel = 1e-4 (the benchmark's stated step) and 1e-5; the misfit has kinks
 (limiter and guard branches), and the difference quotients of the two
 steps differ by more than the smaller one differs from the adjoint.
 
+With --jvp, the existing file's schedule is kept and the exact directional
+derivatives of the same FP64 misfit along each parameter are added to it
+("grad_wind_jvp_fp64"), from the FP64 build run in forward-mode dual
+numbers (oracle/dual.h): the derivative the difference quotients
+approximate, with no step.
+
 Writes adjoint_fd_3x97x97x49.json beside this file; the GPU test
 tests/test_adjoint_gpu.py::test_nested_97_gradient compares the library's
 adjoint with it.
 
     python tests/golden/make_adjoint_fd.py [--params 0,1,..] [--hrel 1e-4,1e-5]
-                                           [--divb-every N] [--errlim E] [--out NAME]
+                                           [--divb-every N] [--errlim E] [--out NAME] [--jvp]
 """
 import json
 import os
@@ -57,7 +63,7 @@ def wind_steps(w, h_rel):
 
 
 def main(argv=()):
-    opts = dict(a.split("=", 1) for a in argv if a.startswith("--"))
+    opts = dict(a.split("=", 1) for a in argv if a.startswith("--") and "=" in a)
     over = {}
     if "--divb-every" in opts:
         over["divb_every"] = int(opts["--divb-every"])
@@ -66,6 +72,8 @@ def main(argv=()):
     comps = [int(x) for x in opts["--params"].split(",")] if "--params" in opts else list(range(8))
     hrels = [float(x) for x in opts["--hrel"].split(",")] if "--hrel" in opts else [1e-4, 1e-5]
     name = opts.get("--out", "adjoint_fd_3x97x97x49.json")
+    if "--jvp" in argv:
+        return add_jvp(name, comps)
     from g3m3_gb300.adjoint import line_samples, wind_of
     from oracle.oracle import OracleModel
     st = adjoint_grid(**over)
@@ -97,6 +105,27 @@ def main(argv=()):
            "wind": w0.tolist(), "loss_fp64": L0, "grad_wind_fd_fp64": grads, "schedule": sch}
     with open(os.path.join(HERE, name), "w") as fh:
         json.dump(out, fh, indent=1)
+    print("written")
+
+
+def add_jvp(name, comps):
+    from g3m3_gb300.adjoint import line_samples, wind_of
+    path = os.path.join(HERE, name)
+    fx = json.load(open(path))
+    st = adjoint_grid()
+    samples = line_samples(st, NSTEPS, n=200)
+    w0 = wind_of(st.params)
+    assert np.array_equal(w0, np.array(fx["wind"]))
+    jvp = fx.get("grad_wind_jvp_fp64", [None] * 8)
+    for k in comps:
+        e = np.zeros(8)
+        e[k] = 1.0
+        t0 = time.time()
+        loss, jvp[k] = R.oracle_jvp(st, w0, fx["schedule"], samples, wind_tangent=e)
+        print(f"w[{k}]: {jvp[k]:.10e} (loss {loss:.10e}, {time.time() - t0:.0f} s)", flush=True)
+        fx["grad_wind_jvp_fp64"] = jvp
+        with open(path, "w") as fh:
+            json.dump(fx, fh, indent=1)
     print("written")
 
 
