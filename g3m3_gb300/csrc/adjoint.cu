@@ -501,10 +501,9 @@ void rev_box(g3m3_adjoint* A, const BoxRec& R) {
   {
     const float* we = A->a_we + (size_t)(b - 1) * n3;
     launch_copy_fields(aW[G3M3_F_EPRES], &we, 1, n3, s);
-    const float* src[G3M3_NFIELDS];
+    float* src[G3M3_NFIELDS];
     for (int q = 0; q < G3M3_NFIELDS; q++) src[q] = aold(A, q, b);
-    launch_copy_fields(A->aO, src, G3M3_NFIELDS, n3, s);
-    for (int q = 0; q < G3M3_NFIELDS; q++) cudaMemsetAsync(aold(A, q, b), 0, n3 * sizeof(float), s);
+    launch_move_fields(A->aO, src, G3M3_NFIELDS, n3, s);
   }
   float *s0[G3M3_NFIELDS], *w1[G3M3_NFIELDS], *c1[G3M3_NFIELDS], *l1[G3M3_NFIELDS];
   tab_of(R.s0, n3, s0);

@@ -224,6 +224,7 @@ void launch_adj_divb_apply(const AdjDivbArgs& a, cudaStream_t s);
 void launch_loss(const LossArgs& a, cudaStream_t s, bool reverse);
 void launch_copy_fields(float* dst, const float* const src[], int nf, size_t n, cudaStream_t s);
 void launch_copy_fields_out(float* const dst[], const float* src, int nf, size_t n, cudaStream_t s);
+void launch_move_fields(float* dst, float* const src[], int nf, size_t n, cudaStream_t s);   // src cleared
 void launch_zero(float* p, size_t n, cudaStream_t s);
 void launch_axpy(float* y, const float* x, size_t n, cudaStream_t s);   // y += x
 

@@ -1297,6 +1297,16 @@ __global__ void k_copy_fields(float* __restrict__ dst, const __grid_constant__ F
     dst[(size_t)f * n + c] = __ldg(src.p[f] + c);
 }
 
+// the fields into a block, each source cleared behind the copy
+__global__ void k_move_fields(float* __restrict__ dst, const __grid_constant__ FieldPtrsW src, int nf, size_t n) {
+  const int f = blockIdx.y;
+  if (f >= nf) return;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    dst[(size_t)f * n + c] = src.p[f][c];
+    src.p[f][c] = 0.0f;
+  }
+}
+
 __global__ void k_copy_fields_out(const __grid_constant__ FieldPtrsW dst, const float* __restrict__ src, int nf,
                                   size_t n) {
   const int f = blockIdx.y;
@@ -1419,6 +1429,13 @@ void launch_copy_fields(float* dst, const float* const src[], int nf, size_t n, 
   for (int f = 0; f < nf; f++) p.p[f] = src[f];
   const unsigned bx = blocks_for(n, 256) < 4u * sm_count() ? blocks_for(n, 256) : 4u * sm_count();
   k_copy_fields<<<dim3(bx, (unsigned)nf), 256, 0, s>>>(dst, p, nf, n);
+}
+
+void launch_move_fields(float* dst, float* const src[], int nf, size_t n, cudaStream_t s) {
+  FieldPtrsW p{};
+  for (int f = 0; f < nf; f++) p.p[f] = src[f];
+  const unsigned bx = blocks_for(n, 256) < 4u * sm_count() ? blocks_for(n, 256) : 4u * sm_count();
+  k_move_fields<<<dim3(bx, (unsigned)nf), 256, 0, s>>>(dst, p, nf, n);
 }
 
 void launch_copy_fields_out(float* const dst[], const float* src, int nf, size_t n, cudaStream_t s) {
