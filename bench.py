@@ -225,6 +225,15 @@ def run_ours(args):
     barrier()
     e2e_s = time.perf_counter() - t0
     cu_e = m.times()[2] - cu_e0
+    # the host link on its own: the whole state up and down (best of 3)
+    up_s = down_s = 1e30
+    for _ in range(3):
+        t0 = time.perf_counter()
+        m.set_state(host_np.reshape(34, p.n_grids, p.nz, p.ny, p.nx))
+        up_s = min(up_s, time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        m.state(out=host_np.reshape(34, p.n_grids, p.nz, p.ny, p.nx))
+        down_s = min(down_s, time.perf_counter() - t0)
 
     # one div B cleaning pass over all boxes (the main-step loop runs one
     # inside every 10th main step, so the timed region above holds one)
@@ -279,7 +288,10 @@ def run_ours(args):
                        "steps": TRIAL},
         "e2e": {"value": cu_e / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": 34 * n4 * 4,
                 "d2h_bytes_per_step": 34 * n4 * 4,
-                "path": "g3m3_model_step_host (pinned host state in, per-box uploads overlapping the step, state out)"},
+                "path": "g3m3_model_step_host (pinned host state in, per-box uploads overlapping the step, state out)",
+                "state_copy_ms": {"h2d": up_s * 1e3, "d2h": down_s * 1e3,
+                                  "note": "the whole state alone, best of 3: the read-back follows the step's last "
+                                          "kernels, and the step waits for the coarsest box's upload"}},
         "gpu_launches": int(k_g),
         "divb_all_ms": divb_ms,
         "roofline": roof,
