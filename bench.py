@@ -230,6 +230,7 @@ def run_ours(args):
     for _ in range(3):
         t0 = time.perf_counter()
         m.set_state(host_np.reshape(34, p.n_grids, p.nz, p.ny, p.nx))
+        torch.cuda.synchronize(local)   # the upload is asynchronous
         up_s = min(up_s, time.perf_counter() - t0)
         t0 = time.perf_counter()
         m.state(out=host_np.reshape(34, p.n_grids, p.nz, p.ny, p.nx))

@@ -96,7 +96,13 @@ struct Off7 {
 // along z with the 13 stencil fields of three planes staged in shared
 // memory (350 against 215 us: two barriers per plane); each thread's 108
 // inputs copied into its own shared-memory column by asynchronous copies
-// issued at once (238 against 215 us: the sweep still holds 168 registers).
+// issued at once (238 against 215 us: the sweep still holds 168 registers);
+// the reverse split into launches over subsets of the ten outputs, each
+// with the sweep of its outputs only (generated per subset; the subsets'
+// gradients sum to the whole cell's): density and momenta, then the six
+// pressures, 9 % slower at 128 registers and 13 % at 168; three parts
+// (momenta, diagonal, off-diagonal pressures) 25 % slower at 128 or 80,
+// since the stencil loads and atomics the parts share are repeated.
 __global__ void __launch_bounds__(128, 3) k_adj_push_ion(const __grid_constant__ AdjPushIonArgs a) {
   const Dims d = a.d;
   const Cell3 p = cell3(d);
