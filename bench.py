@@ -220,8 +220,11 @@ def run_ours(args):
     barrier()
     t0 = time.perf_counter()
     cu_e0 = m.times()[2]
+    call_ms = []
     for _ in range(e2e_steps):
+        tc = time.perf_counter()
         m.step_host(host_np, host_np, graph=use_graph)
+        call_ms.append(round((time.perf_counter() - tc) * 1e3, 2))
     barrier()
     e2e_s = time.perf_counter() - t0
     cu_e = m.times()[2] - cu_e0
@@ -290,6 +293,7 @@ def run_ours(args):
         "e2e": {"value": cu_e / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": 34 * n4 * 4,
                 "d2h_bytes_per_step": 34 * n4 * 4,
                 "path": "g3m3_model_step_host (pinned host state in, per-box uploads overlapping the step, state out)",
+                "ms_per_call": call_ms,
                 "state_copy_ms": {"h2d": up_s * 1e3, "d2h": down_s * 1e3,
                                   "note": "the whole state alone, best of 3: the read-back follows the step's last "
                                           "kernels, and the step waits for the coarsest box's upload"}},
