@@ -785,8 +785,17 @@ __global__ void __launch_bounds__(128) k_adj_guard_b(const __grid_constant__ Adj
 struct OuterA {
   const AdjOuterArgs* a;
   int f, comp;
-  double gp[8];
+  double gp;   // this thread's share of the adjoint of the field's wind parameter
+  bool hit;    // the thread reached the wind face
 };
+
+// The wind parameter a field's wind-face value depends on (k_bndry.cu
+// wind_value): 0 srho, 1-3 the velocity, 4 spress, 5-7 the IMF; -1 none.
+__device__ __forceinline__ int wind_param(int f) {
+  if (f >= 30) return f == G3M3_F_EPRES ? 4 : 5 + (f - G3M3_F_BX);
+  const int q = f % 10;
+  return q == 0 ? 0 : (q <= 3 ? q : (q < 7 ? 4 : -1));
+}
 
 template <int S>
 __device__ float outer_val_a(const OuterA& o, int i, int j, int k) {
@@ -850,8 +859,8 @@ __device__ void wind_adj(OuterA& o, float g) {
   const AdjOuterArgs& a = *o.a;
   const int f = o.f;
   if (f >= 30) {
-    if (f == G3M3_F_EPRES) o.gp[4] += (double)g * 0.5 / (double)a.ti_te;
-    else o.gp[5 + (f - G3M3_F_BX)] += (double)g;
+    o.gp += f == G3M3_F_EPRES ? (double)g * 0.5 / (double)a.ti_te : (double)g;
+    o.hit = true;
     return;
   }
   const int s = f / 10, q = f % 10;
@@ -862,9 +871,8 @@ __device__ void wind_adj(OuterA& o, float g) {
     const float mf = s == 1 ? a.rmassh / a.rmassq : a.rmasso / a.rmassq;
     w = q <= 3 ? (double)fr * (double)mf : (double)fr;
   }
-  if (q == 0) o.gp[0] += w * g;
-  else if (q <= 3) o.gp[q] += w * g;
-  else o.gp[4] += 0.5 * w * g;
+  o.gp += q <= 3 ? w * g : 0.5 * w * g;
+  o.hit = true;
 }
 
 template <int S>
@@ -949,7 +957,8 @@ __global__ void __launch_bounds__(256) k_adj_outer(const __grid_constant__ AdjOu
   o.a = &a;
   o.f = f;
   o.comp = f < 30 ? ((f % 10) >= 1 && (f % 10) <= 3 ? f % 10 : 0) : 0;
-  for (int q = 0; q < 8; q++) o.gp[q] = 0.0;
+  o.gp = 0.0;
+  o.hit = false;
   int i, j, k;
   if (shell1_cell(t, a.d, i, j, k)) {
     const size_t c = a.d.at(i, j, k);
@@ -957,19 +966,24 @@ __global__ void __launch_bounds__(256) k_adj_outer(const __grid_constant__ AdjOu
     a.a[f][c] = 0.0f;   // every shell value was overwritten
     outer_adj<8>(o, i, j, k, g);
   }
-  // block sums of the parameter adjoints, one atomic per block and parameter
-  __shared__ double part[8][8];
+  // block sum of the field's wind-parameter adjoint, one atomic per block;
+  // FP64 is slow on this GPU, so only warps that reached the wind face
+  // reduce
+  const int pidx = wind_param(f);
+  if (pidx < 0) return;   // block-uniform: f is the block's field
+  __shared__ double part[8];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int q = 0; q < 8; q++) {
-    double v = o.gp[q];
+  double v = 0.0;
+  if (__any_sync(0xffffffffu, o.hit)) {
+    v = o.gp;
     for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
-    if (lane == 0) part[q][warp] = v;
   }
+  if (lane == 0) part[warp] = v;
   __syncthreads();
-  if (threadIdx.x < 8) {
-    double v = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); w++) v += part[threadIdx.x][w];
-    if (v != 0.0) atomicAdd(a.a_param + threadIdx.x, v);
+  if (threadIdx.x == 0) {
+    double sum = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) sum += part[w];
+    if (sum != 0.0) atomicAdd(a.a_param + pidx, sum);
   }
 }
 
