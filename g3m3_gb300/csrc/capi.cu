@@ -119,7 +119,7 @@ bool host_floats(g3m3_ctx* c, const float* p, int n, float* out) {
 int ensure_guard_scratch(g3m3_ctx* c, size_t cells) {
   const size_t need = 3 * cells;
   if (!c->words) {
-    G3M3_CUDA(c, dev_alloc(c, (void**)&c->words, 16 * sizeof(unsigned)));
+    G3M3_CUDA(c, dev_alloc(c, (void**)&c->words, 32 * sizeof(unsigned)));
     G3M3_CUDA(c, cudaMallocHost(&c->host_words, 16 * sizeof(unsigned)));
   }
   if (c->guard_cap >= need) return G3M3_OK;
@@ -133,7 +133,7 @@ int ensure_guard_scratch(g3m3_ctx* c, size_t cells) {
 
 int ensure_words(g3m3_ctx* c) {
   if (!c->words) {
-    G3M3_CUDA(c, dev_alloc(c, (void**)&c->words, 16 * sizeof(unsigned)));
+    G3M3_CUDA(c, dev_alloc(c, (void**)&c->words, 32 * sizeof(unsigned)));
     G3M3_CUDA(c, cudaMallocHost(&c->host_words, 16 * sizeof(unsigned)));
   }
   return G3M3_OK;
@@ -319,9 +319,16 @@ __global__ void k_velocity(const float* __restrict__ rho, const float* __restric
   }
 }
 
-__global__ void k_fastest(const unsigned* w, float* out6) {
-  const float px = __uint_as_float(w[1]), py = __uint_as_float(w[2]), pz = __uint_as_float(w[3]);
-  const float cs = __uint_as_float(w[4]), al = __uint_as_float(w[5]);
+// the six results of set_speed_agrd; a word that met a NaN takes its
+// refolded value (the maximum after the last NaN, or NaN)
+__global__ void k_fastest(const unsigned* w, const unsigned* fold, float* out6) {
+  float m[5];
+  for (int q = 0; q < 5; q++) {
+    unsigned bits = w[1 + q];
+    if ((fold[0] >> q) & 1u) bits = ((fold[11] >> q) & 1u) ? fold[6 + q] : 0x7fc00000u;
+    m[q] = __uint_as_float(bits);
+  }
+  const float px = m[0], py = m[1], pz = m[2], cs = m[3], al = m[4];
   out6[0] = px; out6[1] = py; out6[2] = pz; out6[3] = cs; out6[4] = al;
   out6[5] = amax1(0.0f, sqrtf(px * px + py * py + pz * pz + cs * cs + al * al));
 }
@@ -857,14 +864,16 @@ int g3m3_set_speed_agrd(g3m3_ctx* ctx, int nx, int ny, int nz, int n_grids, int 
   a.cslim = cslim; a.iso_flag = ctx->iso_flag; a.isotropic = isotropic != 0;
   a.do_set_rho = 0; a.do_speed = 1;
   a.list = ctx->guard_list; a.list_cap = (unsigned)ctx->guard_cap;
-  a.list_count = ctx->words; a.maxbits = ctx->words + 1;
-  G3M3_CUDA(ctx, cudaMemsetAsync(ctx->words, 0, 16 * sizeof(unsigned), ctx->stream));
+  a.list_count = ctx->words; a.maxbits = ctx->words + 1; a.fold = ctx->words + 16;
+  G3M3_CUDA(ctx, cudaMemsetAsync(ctx->words, 0, 32 * sizeof(unsigned), ctx->stream));
   launch_guards(a, ctx->stream);
+  launch_guard_fold_species(a, ctx->stream);
   ScatterArgs sa{};
   for (int f = 0; f < G3M3_NFIELDS; f++) sa.f[f] = a.f[f];
   sa.list = a.list; sa.list_count = a.list_count; sa.list_cap = a.list_cap;
   launch_guard_scatter(sa, ctx->stream);
-  k_fastest<<<1, 1, 0, ctx->stream>>>(ctx->words, reinterpret_cast<float*>(ctx->words + 8));
+  launch_guard_fold_alf(a, ctx->stream);
+  k_fastest<<<1, 1, 0, ctx->stream>>>(ctx->words, ctx->words + 16, reinterpret_cast<float*>(ctx->words + 8));
   G3M3_CUDA(ctx, cudaMemcpyAsync(ctx->host_words, ctx->words, 16 * sizeof(unsigned), cudaMemcpyDeviceToHost,
                                  ctx->stream));
   G3M3_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

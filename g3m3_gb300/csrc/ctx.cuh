@@ -30,7 +30,7 @@ struct g3m3_ctx {
   int cg_hint = 0;                    // iterations of the last converged CG solve (graph-replayed)
   int cg_hint_plain = 0;              // the same for solves issued as plain launches
   int cg_maxit = 0;                   // iteration cap of every solve (0: the reference's 10 npts)
-  unsigned* words = nullptr;          // [0] list count, [1..5] maxima
+  unsigned* words = nullptr;          // [0] list count, [1..5] maxima, [8..13] set_speed_agrd results, [16..27] GuardArgs::fold
   unsigned* host_words = nullptr;     // pinned
   g3m3::CgState* cg = nullptr;
   g3m3::CgState* host_cg = nullptr;   // pinned

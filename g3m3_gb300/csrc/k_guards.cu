@@ -50,6 +50,23 @@ __device__ __forceinline__ Sp load_diag(const GuardArgs& a, int s, size_t c) {
   return v;
 }
 
+// The limiter's speeds of one species at one cell
+// (sub_set_speed_agrd.f90:135-141): |p|/(rho + smallbit) per component and
+// the sound speed
+struct Speeds {
+  float vx, vy, vz, cq;
+};
+
+__device__ __forceinline__ Speeds speeds(const Sp& v, float smallbit) {
+  const float arho = v.r + smallbit;
+  Speeds o;
+  o.vx = fabsf(v.px / arho);
+  o.vy = fabsf(v.py / arho);
+  o.vz = fabsf(v.pz / arho);
+  o.cq = sqrtf(0.33f * (v.xx + v.yy + v.zz) / arho);
+  return o;
+}
+
 __device__ __forceinline__ float rho_min(int s) { return s == 0 ? 2.e-4f : (s == 1 ? 1.e-4f : 2.e-5f); }
 
 // set_rho for one species; returns true when the values changed
@@ -125,10 +142,14 @@ __global__ void __launch_bounds__(256, 4) k_guards(const __grid_constant__ Guard
         if (floored) append(a, c, s, v);   // deferred: neighbours still read this cell
         continue;
       }
-      const float arho = v.r + a.smallbit;
-      const float avx = fabsf(v.px / arho), avy = fabsf(v.py / arho), avz = fabsf(v.pz / arho);
+      const Speeds sv = speeds(v, a.smallbit);
+      const float avx = sv.vx, avy = sv.vy, avz = sv.vz, cq = sv.cq;
       const float vq = sqrtf(avx * avx + avy * avy + avz * avz);
-      const float cq = sqrtf(0.33f * (v.xx + v.yy + v.zz) / arho);
+      if (a.fold) {
+        const unsigned nan_bits = (isnan(avx) ? 1u : 0u) | (isnan(avy) ? 2u : 0u) | (isnan(avz) ? 4u : 0u) |
+                                  (isnan(cq) ? 8u : 0u);
+        if (nan_bits) atomicOr(a.fold, nan_bits);
+      }
       const float vl = a.vlim * a.svlim[s];
       const float cl = a.vlim * a.svlim[s] * a.sclim[s];
       if ((vq > vl) || (cq > cl)) {
@@ -183,7 +204,9 @@ __global__ void __launch_bounds__(256, 4) k_guards(const __grid_constant__ Guard
         const float arho = newr[0] + newr[1] + newr[2] + a.smallbit;
         const float cs = sqrtf(ep / arho);
         if (cs > a.cslim) { ep = ep * a.cslim / cs; ep_changed = true; }
-        ma = amax1(ma, bt / sqrtf(arho));
+        const float alf = bt / sqrtf(arho);
+        if (a.fold && isnan(alf)) atomicOr(a.fold, 16u);
+        ma = amax1(ma, alf);
       }
     }
     if (ep_changed) a.f[G3M3_F_EPRES][c] = ep;
@@ -203,6 +226,72 @@ __global__ void __launch_bounds__(256, 4) k_guards(const __grid_constant__ Guard
 #pragma unroll
       for (int w = 1; w < 8; w++) m = amax1(m, wmax[tid][w]);
       if (m > 0.0f) atomicMax(a.maxbits + tid, __float_as_uint(m));
+    }
+  }
+}
+
+// The reference folds its maxima in loop order with amax1 (a > b ? a : b):
+// a NaN replaces the running value and the next element replaces the NaN,
+// so the result is the maximum of the elements after the last NaN (NaN when
+// the NaN is the last element).  The words that met a NaN in k_guards are
+// refolded here, in two passes: the last NaN's position, then the maximum
+// after it.  Species words (pxmax..csmax) run over the species loops
+// (species, then k, j, i over interior cells) on the values k_guards read,
+// so before the scatter; alfmax over interior cells on the densities after
+// the limiter, so after it.
+__device__ __forceinline__ bool interior_cell(const Dims& d, long t, int& i, int& j, int& k) {
+  const long ix = d.nx - 2, iy = d.ny - 2;
+  if (t >= ix * iy * (d.nz - 2)) return false;
+  i = (int)(t % ix) + 2;
+  j = (int)((t / ix) % iy) + 2;
+  k = (int)(t / (ix * iy)) + 2;
+  return true;
+}
+
+template <int PASS>
+__global__ void __launch_bounds__(256) k_fold_species(const __grid_constant__ GuardArgs a) {
+  const unsigned flag = *(volatile unsigned*)a.fold & 15u;
+  if (!flag) return;
+  const Dims d = a.d;
+  const long nint = (long)(d.nx - 2) * (d.ny - 2) * (d.nz - 2);
+  int i, j, k;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; interior_cell(d, t, i, j, k);
+       t += (long)gridDim.x * blockDim.x) {
+    const size_t c = d.at(i, j, k);
+    for (int s = 0; s < 3; s++) {
+      const Speeds sv = speeds(load_diag(a, s, c), a.smallbit);
+      const float x[4] = {sv.vx, sv.vy, sv.vz, sv.cq};
+      const unsigned pos = (unsigned)(s * nint + t + 1);
+#pragma unroll
+      for (int w = 0; w < 4; w++) {
+        if (!((flag >> w) & 1u)) continue;
+        if (PASS == 0) {
+          if (isnan(x[w])) atomicMax(a.fold + 1 + w, pos);
+        } else if (pos > *(volatile unsigned*)(a.fold + 1 + w)) {
+          atomicMax(a.fold + 6 + w, x[w] == 0.0f ? 0u : __float_as_uint(x[w]));
+          atomicOr(a.fold + 11, 1u << w);
+        }
+      }
+    }
+  }
+}
+
+template <int PASS>
+__global__ void __launch_bounds__(256) k_fold_alf(const __grid_constant__ GuardArgs a) {
+  if (!(*(volatile unsigned*)a.fold & 16u)) return;
+  const Dims d = a.d;
+  int i, j, k;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; interior_cell(d, t, i, j, k);
+       t += (long)gridDim.x * blockDim.x) {
+    const size_t c = d.at(i, j, k);
+    const float arho = a.f[0][c] + a.f[10][c] + a.f[20][c] + a.smallbit;
+    const float x = a.btot[c] / sqrtf(arho);
+    const unsigned pos = (unsigned)(t + 1);
+    if (PASS == 0) {
+      if (isnan(x)) atomicMax(a.fold + 5, pos);
+    } else if (pos > *(volatile unsigned*)(a.fold + 5)) {
+      atomicMax(a.fold + 10, x == 0.0f ? 0u : __float_as_uint(x));
+      atomicOr(a.fold + 11, 16u);
     }
   }
 }
@@ -229,6 +318,16 @@ __global__ void __launch_bounds__(256) k_copy(float* __restrict__ dst, const flo
 void launch_guards(const GuardArgs& a, cudaStream_t s) {
   const dim3 blk(32, 4, 2), grd = grid3(a.d, blk);
   k_guards<<<grd, blk, 0, s>>>(a);
+}
+
+void launch_guard_fold_species(const GuardArgs& a, cudaStream_t s) {
+  k_fold_species<0><<<sm_count(), 256, 0, s>>>(a);
+  k_fold_species<1><<<sm_count(), 256, 0, s>>>(a);
+}
+
+void launch_guard_fold_alf(const GuardArgs& a, cudaStream_t s) {
+  k_fold_alf<0><<<sm_count(), 256, 0, s>>>(a);
+  k_fold_alf<1><<<sm_count(), 256, 0, s>>>(a);
 }
 
 void launch_guard_scatter(const ScatterArgs& a, cudaStream_t s) {

@@ -136,6 +136,12 @@ struct GuardArgs {         // set_rho and/or set_speed_agrd
   unsigned int* list_count;
   unsigned int list_cap;
   unsigned int* maxbits;   // 5 words: pxmax pymax pzmax csmax alfmax (float bits)
+  // The reference's running maximum restarts after a NaN; the drop-in
+  // reproduces that through these words (null: plain maxima): [0] bit w set
+  // when word w met a NaN, [1+w] the last NaN's position in the
+  // reference's loop order + 1, [6+w] the maximum after it (float bits),
+  // [11] bit w set when an element follows it.
+  unsigned int* fold;
 };
 
 struct ScatterArgs {

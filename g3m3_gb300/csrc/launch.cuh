@@ -44,6 +44,10 @@ cudaError_t prepare_fcsmooth();   // once, outside stream capture
 // k_guards.cu
 void launch_guards(const GuardArgs& a, cudaStream_t s);
 void launch_guard_scatter(const ScatterArgs& a, cudaStream_t s);
+// set_speed_agrd's maxima where one met a NaN, in the reference's loop order
+// (GuardArgs::fold): the species words before the scatter, alfmax after it
+void launch_guard_fold_species(const GuardArgs& a, cudaStream_t s);
+void launch_guard_fold_alf(const GuardArgs& a, cudaStream_t s);
 void launch_copy(float* dst, const float* src, size_t n, cudaStream_t s);
 
 }  // namespace g3m3

@@ -283,6 +283,51 @@ def c_set_speed_agrd(side, box):
     return uniform(side, "set_speed_agrd", args, scalars=6)
 
 
+def nan_speed_inputs(I, box, plant):
+    """Cells whose limiter speeds are NaN or infinite: density -smallbit
+    (rho + smallbit = 0) with zero momenta and pressures gives NaN, with a
+    momentum gives inf; three negative densities give a NaN Alfven speed.
+    The reference folds its maxima in loop order with amax1, so a NaN resets
+    the running value: 'last' puts the NaN on the last element of the
+    species loops, 'mid' an inf and then a NaN in the first species and
+    the Alfven NaN halfway through."""
+    p = I.p
+    c = I.cur
+    b = box - 1
+    sb = np.float32(-np.float32(p.smallbit))
+
+    def nan_cell(s, k, j, i, px=0.0):
+        c[s + 0, b, k, j, i] = sb
+        c[s + 1, b, k, j, i] = px
+        c[s + 2, b, k, j, i] = 0.0
+        c[s + 3, b, k, j, i] = 0.0
+        for q in (4, 5, 6):
+            c[s + q, b, k, j, i] = 0.0
+
+    nz, ny, nx = p.nz, p.ny, p.nx
+    if plant == "last":
+        nan_cell(20, nz - 2, ny - 2, nx - 2)
+    else:
+        nan_cell(0, 2, 3, 4, px=5.0)          # inf, then
+        nan_cell(0, nz // 2, ny // 2, 5)      # NaN in the first species loop
+        for s in (0, 10, 20):                 # the Alfven speed's NaN
+            c[s, b, nz // 2, ny // 2 + 1, 3] = -1.0
+
+
+def c_set_speed_agrd_nan(side, box, plant):
+    """The maxima where speeds are NaN or infinite (nan_speed_inputs)."""
+    I = Inputs("tiny2")
+    nan_speed_inputs(I, box, plant)
+    p = I.p
+    f = I.cur
+    vlim = p.vlim_factor * box
+    args = (I.dims(box) + [p.rmassq, p.rmassh, p.rmasso, 0, p.smallbit, p.aniso_limit, vlim, p.qvlim,
+                           p.hvlim, p.ovlim, p.qclim, p.hclim, p.oclim, p.cslim,
+                           f[31], f[32], f[33], I.b0[0], I.b0[1], I.b0[2]]
+            + [f[q] for q in range(30)] + [f[30], np.zeros(I.box3, np.float32)])
+    return uniform(side, "set_speed_agrd", args, scalars=6)
+
+
 def c_store_array(side):
     I = Inputs("tiny2")
     return uniform(side, "store_array", [I.old[0], I.cur[0]] + I.dims(2))
@@ -532,6 +577,8 @@ for _box in (1, 2):
     _add(c_flux_correct, box=_box)
     _add(c_set_rho, box=_box)
     _add(c_set_speed_agrd, box=_box)
+    for _plant in ("last", "mid"):
+        _add(c_set_speed_agrd_nan, box=_box, plant=_plant)
     _add(c_flux_counter, box=_box)
     _add(c_bndry_flanks, box=_box)
     _add(c_bndry_corer, box=_box)

@@ -79,6 +79,25 @@ class Inputs:
         self.lists = self.st.lists
         self.resistive = self.st.resistive.copy()
 
+    def crop(self, nx, ny, nz):
+        """Keep the first nx x ny x nz cells of every box: an anisotropic box
+        whose sizes leave ragged tiles in every direction.  Each box keeps
+        its spacing; its upper extents follow.  The inner-boundary lists no
+        longer apply."""
+        p = self.p
+        assert nx <= p.nx and ny <= p.ny and nz <= p.nz
+        for name in ("cur", "old", "wrk", "b0"):
+            setattr(self, name, np.ascontiguousarray(getattr(self, name)[:, :, :nz, :ny, :nx]))
+        self.resistive = np.ascontiguousarray(self.resistive[:, :nz, :ny, :nx])
+        for b in range(p.n_grids):
+            for ax, n_old, n_new in (("x", p.nx, nx), ("y", p.ny, ny), ("z", p.nz, nz)):
+                lo, hi = getattr(p, f"grd_{ax}min"), getattr(p, f"grd_{ax}max")
+                hi[b] = lo[b] + (hi[b] - lo[b]) / (n_old - 1) * (n_new - 1)
+        p.nx, p.ny, p.nz = nx, ny, nz
+        self.box3 = (nz, ny, nx)
+        self.lists = None
+        return self
+
     def scratch(self, scale=1.0, n=1):
         return [(scale * self.rng.standard_normal(self.box3)).astype(np.float32) for _ in range(n)]
 

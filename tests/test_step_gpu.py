@@ -145,6 +145,20 @@ def test_fcsmooth_variants(cfg, nsteps, variant):
     assert np.array_equal(tsn, om.t_stepnew)
 
 
+@pytest.mark.parametrize("limit", [22, 14])
+@pytest.mark.parametrize("variant", range(8))
+def test_ragged_grids_every_variant(limit, variant):
+    """Three nested boxes of 45x45x23 or 29x29x15 (remainders 13 and 29
+    against the 32-wide tile rows, 5 and 13 against 8- and 16-row tiles,
+    where the other grids leave 1): two main steps with each flux-correction
+    form, every kernel of the step on ragged tiles, bitwise."""
+    om, g, (t, tsn, cu, k, gl) = run_pair("tiny3", 2, variant=variant, limit=limit)
+    for q in range(34):
+        assert_same(g[q], om.cur[q], f"limit {limit} variant {variant} field {q}")
+    assert np.array_equal(tsn, om.t_stepnew)
+    assert cu == om.cell_updates
+
+
 @pytest.mark.parametrize("graph,pin", [(False, True), (True, True), (False, False)])
 def test_step_host(graph, pin):
     """Host-fed main steps (per-box uploads overlapping the step, result
