@@ -63,17 +63,18 @@ def test_wind_gradient_against_fp64_differences(cfg, nsteps, every, divb):
     assert err <= GRAD_TOL, (err, ga, fd)
 
 
-@pytest.mark.parametrize("divb", [0, 2])
-def test_gradient_against_fp64_forward_mode(divb):
+@pytest.mark.parametrize("divb,limit", [(0, 8), (2, 8), (0, 14), (2, 14)])
+def test_gradient_against_fp64_forward_mode(divb, limit):
     """The wind and state gradients against exact directional derivatives of
     the same misfit: the oracle's FP64 build in forward-mode dual numbers
     (oracle/dual.h) under the same schedule, one run per direction, with no
     difference step (so no limiter kink biases it).  Bar: 1e-4 relative L2
     over the eight wind parameters and 1e-4 relative on a random direction
     of all 34 fields (measured about 1e-7 and 1e-6 without div B: the FP32
-    run and the FP64 run take the same branches)."""
+    run and the FP64 run take the same branches).  Boxes of 17x17x9 and,
+    ragged against every tile shape of the reverse kernels, 29x29x15."""
     over = dict(divb_every=divb, divb_errlim=1e-6) if divb else dict(divb_every=0)
-    ctx, st, samples, run = _run("tiny3", 4, 2, **over)
+    ctx, st, samples, run = _run("tiny3", 4, 2, limit=limit, **over)
     w = R.wind_of(st)
     run.loss(w)
     sch = run.schedule
