@@ -1,7 +1,8 @@
 """Drop-in routines on anisotropic boxes whose sizes leave ragged tiles in
 every direction (nx, ny, nz all different; remainders 13, 5 and 1 against
 the 32-wide tile rows, 5 and 9 against 8- and 16-row tiles, 17 and 5
-interior planes), against the oracle, bitwise.  The boxes are the first
+interior planes), against the oracle, bitwise (div B: against the FP64
+build, as its drop-in test states).  The boxes are the first
 cells of each box of the three-box 49x49x25 grid (Inputs.crop); the first
 and the last box of the array are used, so the per-box offsets are
 exercised too."""
@@ -120,3 +121,11 @@ def test_guards_ragged(shape, box):
         assert_same(ga[k], oa[k], f"set_speed_agrd arg {k}")
     for x, y, n in zip(go, oo, ("pxmax", "pymax", "pzmax", "csmax", "alfmax", "fastest")):
         assert x.value == y.value, (n, x.value, y.value)
+
+
+@pytest.mark.parametrize("shape,box", CASES)
+def test_divb_correct_ragged(shape, box):
+    """The div B projection on the anisotropic boxes: the bar of
+    test_routines_gpu.py::test_divb_correct (B at least as close to the
+    FP64 solve as the reference's FP32 solve, residual, iteration count)."""
+    R.check_divb(ragged(shape), box, 1e-4)

@@ -300,9 +300,11 @@ def test_divb_correct(cfg, errlim):
     """Compared with the FP64 build: the oracle sums dot products serially
     in FP32 as the reference does, the library in FP64; the library's B must
     be as close to the FP64 solve as the reference's (tests/_divb_parity.py)."""
-    I = Inputs(cfg)
+    check_divb(Inputs(cfg), 1, errlim)
+
+
+def check_divb(I, box, errlim):
     p = I.p
-    box = 1
     pos = (ctypes.c_int * 7)(p.nx * p.ny, p.nx, 1, 0, -1, -p.nx, -p.nx * p.ny)
     xs = np.array(p.xspac[: p.n_grids], np.float32)
     b = [I.cur[31].copy(), I.cur[32].copy(), I.cur[33].copy()]
