@@ -129,3 +129,37 @@ def test_divb_correct_ragged(shape, box):
     test_routines_gpu.py::test_divb_correct (B at least as close to the
     FP64 solve as the reference's FP32 solve, residual, iteration count)."""
     R.check_divb(ragged(shape), box, 1e-4)
+
+
+def _inside_coarser(I, box):
+    """The box's cells interpolate from cells of box+1 that exist."""
+    p = I.p
+    for ax, n in (("x", p.nx), ("y", p.ny), ("z", p.nz)):
+        lo_f, hi_f = getattr(p, f"grd_{ax}min")[box - 1], getattr(p, f"grd_{ax}max")[box - 1]
+        lo_c, hi_c = getattr(p, f"grd_{ax}min")[box], getattr(p, f"grd_{ax}max")[box]
+        dc = (hi_c - lo_c) / (n - 1)
+        if not (lo_f >= lo_c and (hi_f - lo_c) / dc + 2 <= n):
+            return False
+    return True
+
+
+@pytest.mark.parametrize("box", [1, 2])
+def test_flanks_and_corer_ragged(box):
+    """flanks, corer and flanks_synced between a 45x29x19 box and its
+    coarser neighbour (cut from the same grid, so the finer box still lies
+    inside the coarser one)."""
+    I = ragged((45, 29, 19))
+    assert _inside_coarser(I, box)
+    p = I.p
+    g = I.grid()
+    t_old = (ctypes.c_double * p.n_grids)(*([0.0] * p.n_grids))
+    t_new = (ctypes.c_double * p.n_grids)(*([0.2] * p.n_grids))
+    work = np.zeros(I.box3, np.float32)
+    for q in (0, 7, 33):
+        args = [I.wrk[q], I.cur[q], I.old[q]] + I.dims(box) + [t_new, t_old, 0.07, work] + g
+        oa, ga = run_both("flanks", args)
+        assert_same(ga[0], oa[0], f"flanks box {box} field {q}")
+        oa, ga = run_both("corer", [I.cur[q]] + I.dims(box) + g)
+        assert_same(ga[0], oa[0], f"corer box {box} field {q}")
+        oa, ga = run_both("flanks_synced", [I.cur[q]] + I.dims(box) + g)
+        assert_same(ga[0], oa[0], f"flanks_synced box {box} field {q}")
