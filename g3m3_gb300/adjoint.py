@@ -16,6 +16,10 @@ CUDA adjoint, so
 
     loss = WindMisfit.apply(upstream_wind(u, setup), run)
     loss.backward()            # u.grad = dL/d(n, vx, vy, vz, bx, by, bz)
+
+``EnsembleWindMisfit`` is the batched form over the members of an
+``Ensemble`` (``EnsembleMisfit``): one loss per member, each member's
+gradient from its own adjoint.
 """
 from __future__ import annotations
 
@@ -198,15 +202,19 @@ class MisfitRun:
     samples and (after the first call) the time-step schedule; ``loss(w)``
     runs it with wind parameters w and keeps the adjoint ready."""
 
-    def __init__(self, model: Model, state, nsteps, samples, checkpoint_every=10, cg_errlim=0.0, schedule=None):
+    def __init__(self, model: Model, state, nsteps, samples, checkpoint_every=10, cg_errlim=0.0, schedule=None,
+                 clock=None):
         self.model = model
         self.state = state
         self.adj = Adjoint(model, nsteps, checkpoint_every, cg_errlim)
         self.adj.set_samples(*samples)
         self.schedule = schedule
+        # every run starts from this clock (t, main steps done: the div B cadence)
+        self.clock = model.clock() if clock is None else clock
 
     def reset(self):
         self.model.upload(self.state)
+        self.model.set_clock(*self.clock)
         self.model.init_steps()
 
     def loss(self, wind):
@@ -252,6 +260,46 @@ def ensemble_gradients(ensemble, states, nsteps, samples_of, checkpoint_every=1,
     return out
 
 
+class EnsembleMisfit:
+    """The batched experiment: the members of an ``Ensemble``, each from
+    its own state and its clock at construction, N main steps, each with its
+    own samples (``samples_of(state)``); the time-step schedules of the
+    first run are kept and reused."""
+
+    def __init__(self, ensemble, states, nsteps, samples_of, checkpoint_every=1, cg_errlim=0.0):
+        self.ensemble = ensemble
+        self.states = list(states)
+        self.nsteps = nsteps
+        self.samples = [samples_of(st) for st in self.states]
+        self.every = checkpoint_every
+        self.errlim = cg_errlim
+        self.schedules = [None] * len(self.states)
+        self.clocks = [m.clock() for m in ensemble.members]
+
+    def member(self, i):
+        """A MisfitRun of member i (its adjoint holds a tape until closed)."""
+        return MisfitRun(self.ensemble.members[i], self.states[i], self.nsteps, self.samples[i], self.every,
+                         self.errlim, schedule=self.schedules[i], clock=self.clocks[i])
+
+    def losses(self, winds):
+        out = []
+        for i in range(len(self.states)):
+            run = self.member(i)
+            out.append(run.loss(winds[i]))
+            self.schedules[i] = run.schedule
+            run.adj.close()
+        return out
+
+    def gradients(self, winds):
+        out = []
+        for i in range(len(self.states)):
+            run = self.member(i)
+            run.loss(winds[i])
+            out.append(run.adj.backward(state=False)["params"])
+            run.adj.close()
+        return out
+
+
 def _function():
     import torch
 
@@ -270,14 +318,41 @@ def _function():
             grads = ctx.run.adj.backward(state=False)
             return torch.from_numpy(grads["params"]) * g, None
 
-    return WindMisfit
+    class EnsembleWindMisfit(torch.autograd.Function):
+        """losses[m] = member m's misfit with wind parameters winds[m]
+        (winds: members x 8) over an EnsembleMisfit; backward: each
+        member's hand-written CUDA adjoint, the members one after another.
+        The forward keeps no tape: backward runs each member's forward
+        again with checkpoints before its reverse, so the members share the
+        memory of one tape."""
+
+        @staticmethod
+        def forward(ctx, winds, experiment):
+            w = winds.detach().cpu().numpy()
+            ctx.experiment = experiment
+            ctx.w = w
+            return torch.tensor(experiment.losses(w), dtype=torch.float64)
+
+        @staticmethod
+        def backward(ctx, g):
+            grads = np.stack(ctx.experiment.gradients(ctx.w))
+            return torch.from_numpy(grads) * g.reshape(-1, 1), None
+
+    return WindMisfit, EnsembleWindMisfit
 
 
 class _Lazy:
-    fn = None
+    fns = None
 
 
 def WindMisfit():
-    if _Lazy.fn is None:
-        _Lazy.fn = _function()
-    return _Lazy.fn
+    if _Lazy.fns is None:
+        _Lazy.fns = _function()
+    return _Lazy.fns[0]
+
+
+def EnsembleWindMisfit():
+    """The batched form of WindMisfit (see _function)."""
+    if _Lazy.fns is None:
+        _Lazy.fns = _function()
+    return _Lazy.fns[1]

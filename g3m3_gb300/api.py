@@ -251,6 +251,17 @@ class Model:
         self.ctx.check(self.L.g3m3_model_times(self.h, ctypes.byref(t), tsn, ctypes.byref(cu)))
         return t.value, np.array(tsn[:]), cu.value
 
+    def clock(self):
+        """(t, main steps done): the time and the count the div B cadence
+        follows."""
+        t = ctypes.c_double()
+        n = ctypes.c_int()
+        self.ctx.check(self.L.g3m3_model_get_clock(self.h, ctypes.byref(t), ctypes.byref(n)))
+        return t.value, n.value
+
+    def set_clock(self, t, nsteps_done):
+        self.ctx.check(self.L.g3m3_model_set_clock(self.h, float(t), int(nsteps_done)))
+
     def stats(self):
         k = ctypes.c_int64()
         g = ctypes.c_int64()

@@ -1752,6 +1752,20 @@ int g3m3_model_times(g3m3_model* m, double* t, double* t_stepnew, int64_t* cell_
   return G3M3_OK;
 }
 
+int g3m3_model_get_clock(g3m3_model* m, double* t, int* nsteps_done) {
+  if (!m) return G3M3_ERR_ARG;
+  if (t) *t = m->t;
+  if (nsteps_done) *nsteps_done = m->nsteps_done;
+  return G3M3_OK;
+}
+
+int g3m3_model_set_clock(g3m3_model* m, double t, int nsteps_done) {
+  if (!m || nsteps_done < 0) return G3M3_ERR_ARG;
+  m->t = t;
+  m->nsteps_done = nsteps_done;
+  return G3M3_OK;
+}
+
 int g3m3_model_stats(g3m3_model* m, int64_t* kernels, int64_t* graphs) {
   if (!m) return G3M3_ERR_ARG;
   if (kernels) *kernels = m->kernels;

@@ -564,6 +564,12 @@ int g3m3_model_autotune(g3m3_model* m, int* fcs_variant);
 /* Time bookkeeping: t, t_stepnew(1..n_grids), executed cell-updates. */
 int g3m3_model_times(g3m3_model* m, double* t, double* t_stepnew,
     int64_t* cell_updates);
+/* The model's clock: the simulation time t and the main steps done, whose
+ * count sets the div B cadence (a pass after every divb_every-th main
+ * step).  Restoring a clock read before a run repeats the run's schedule of
+ * div B passes from the same state. */
+int g3m3_model_get_clock(g3m3_model* m, double* t, int* nsteps_done);
+int g3m3_model_set_clock(g3m3_model* m, double t, int nsteps_done);
 /* Launch counters of the last g3m3_model_run (kernels, graph launches). */
 int g3m3_model_stats(g3m3_model* m, int64_t* kernels, int64_t* graphs);
 /* Stream of the model (for CUDA-event timing by the caller). */

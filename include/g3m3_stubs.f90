@@ -1240,6 +1240,20 @@ module g3m3_c
       real(c_double) :: t_stepnew(*)
       integer(c_int64_t) :: cell_updates
     end function g3m3_model_times
+    function g3m3_model_get_clock(m, t, nsteps_done) bind(C, name="g3m3_model_get_clock")
+      import
+      integer(c_int) :: g3m3_model_get_clock
+      type(c_ptr), value :: m
+      real(c_double) :: t
+      integer(c_int) :: nsteps_done(*)
+    end function g3m3_model_get_clock
+    function g3m3_model_set_clock(m, t, nsteps_done) bind(C, name="g3m3_model_set_clock")
+      import
+      integer(c_int) :: g3m3_model_set_clock
+      type(c_ptr), value :: m
+      real(c_double), value :: t
+      integer(c_int), value :: nsteps_done
+    end function g3m3_model_set_clock
     function g3m3_model_stats(m, kernels, graphs) bind(C, name="g3m3_model_stats")
       import
       integer(c_int) :: g3m3_model_stats

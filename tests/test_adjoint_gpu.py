@@ -250,3 +250,42 @@ def test_ensemble_gradients_match_single_members():
         assert loss == g["loss"]
         assert np.allclose(g["grad_wind"], want, rtol=1e-6, atol=1e-9 * np.abs(want).max()), (want, g["grad_wind"])
         assert np.abs(want).max() > 0
+
+
+def test_ensemble_autograd_matches_ensemble_gradients():
+    """EnsembleWindMisfit (torch.autograd over the members of an Ensemble):
+    the losses equal ensemble_gradients' bit for bit and winds.grad its
+    gradients scaled by the upstream gradient, to 1e-6 (atomic order)."""
+    import torch
+    from g3m3_gb300.adjoint import EnsembleMisfit, EnsembleWindMisfit, ensemble_gradients, line_samples, wind_of
+    from g3m3_gb300.api import Context, Ensemble
+    from g3m3_gb300.state import ensemble_member
+    states = [ensemble_member(i, limits=(8,), n_grids=3, divb_every=2, divb_errlim=1e-6) for i in range(2)]
+    samples_of = lambda st: line_samples(st, 3, n=30)
+    with Context() as ctx:
+        ens = Ensemble(ctx, states)
+        exp = EnsembleMisfit(ens, states, 3, samples_of, checkpoint_every=1)   # the members' clocks at 0
+        want = ensemble_gradients(ens, states, 3, samples_of, checkpoint_every=1)
+        winds = torch.tensor(np.stack([wind_of(st.params) for st in states]), dtype=torch.float64,
+                             requires_grad=True)
+        losses = EnsembleWindMisfit().apply(winds, exp)
+        (losses * torch.tensor([1.0, 2.0], dtype=torch.float64)).sum().backward()
+        ens.close()
+    for i, w in enumerate(want):
+        assert float(losses[i].detach()) == w["loss"]
+        g = winds.grad[i].numpy() / (1.0 + i)
+        assert np.allclose(g, w["grad_wind"], rtol=1e-6, atol=1e-9 * np.abs(w["grad_wind"]).max()), (g, w)
+
+
+def test_misfit_run_repeats_with_div_b_cadence():
+    """A MisfitRun called twice runs the same experiment: its clock (the
+    main-step count the div B cadence follows) is restored with the state,
+    here with 3 main steps and div B every 2, which a second run starting
+    at count 3 would move."""
+    ctx, st, samples, run = _run("tiny3", 3, 1, divb_every=2, divb_errlim=1e-6)
+    w = R.wind_of(st)
+    a = run.loss(w)
+    b = run.loss(w)
+    assert run.model.clock()[1] == 3
+    ctx.close()
+    assert a == b, (a, b)
