@@ -22,7 +22,23 @@ struct InnerArgs {          // bndry_inner on box mbndry
   int mbndry, box;
   Dims d;
   float xmin, ymin, dx, dy, re_equiv, v_rot;
+  int only;                 // 0: the three lists at once; l + 1: list l alone
+  int serial;               // with only: one thread walks the list in order
 };
+
+// How the inner-boundary lists of one box must be applied.  The reference
+// runs the srf, mid and zero lists one after another, each in order, so a
+// cell named twice ends with its last entry's values.  The lists its own
+// set-up builds name each cell once; then every entry can run at once.
+struct InnerOrder {
+  bool overlap = false;                     // a cell in two lists: the lists in turn
+  bool repeat[3] = {false, false, false};   // a cell twice in list l: list l in order
+  bool any() const { return overlap || repeat[0] || repeat[1] || repeat[2]; }
+};
+
+// ij: host copies of the three (mbndry,3,m) lists; entries outside the box
+// are skipped by the kernels and ignored here
+InnerOrder inner_order(const int* const ij[3], const int num[3], int mbndry, int box, const Dims& d);
 
 enum FlanksMode { FLANKS_PLAIN = 0, FLANKS_KEEP = 1, FLANKS_REUSE = 2 };
 
@@ -62,7 +78,8 @@ struct SyncedArgs {         // flanks_synced
 
 long shell_count(const Dims& d, int D);
 void launch_bndry_outer(const OuterArgs& a, cudaStream_t s);
-void launch_bndry_inner(const InnerArgs& a, cudaStream_t s);
+// returns the number of launches (1, or one per nonempty list when o.any())
+int launch_bndry_inner(const InnerArgs& a, const InnerOrder& o, cudaStream_t s);
 void launch_flanks(const FlanksArgs& a, cudaStream_t s);
 void launch_corer(const CorerArgs& a, cudaStream_t s);
 void launch_flanks_synced(const SyncedArgs& a, cudaStream_t s);

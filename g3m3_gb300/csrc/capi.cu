@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstring>
+#include <vector>
 
 #include "ctx.cuh"
 
@@ -670,10 +671,21 @@ int g3m3_bande(g3m3_ctx* ctx, float* efldx, float* efldy, float* efldz, const fl
     if (r.st) return r.st;
     const int counts[2] = {nm[box - 1], nzr[box - 1]};
     const int caps[2] = {mmid, mzero};
+    // a list naming a cell twice adds to it twice, in order: find those on the host
+    const int* lp[2] = {ijmid, ijzero};
+    std::vector<int> hl[2];
     for (int q = 0; q < 2; q++) {
       if (counts[q] < 0 || counts[q] > caps[q]) return set_err(ctx, G3M3_ERR_ARG, "list count out of range");
+      hl[q].resize((size_t)mbndry * 3 * counts[q] + 1);
+      if (counts[q] > 0 && (st = host_ints(ctx, lp[q], mbndry * 3 * counts[q], hl[q].data()))) return st;
+    }
+    const int* hp[3] = {nullptr, hl[0].data(), hl[1].data()};
+    const int num3[3] = {0, counts[0], counts[1]};
+    const InnerOrder order = inner_order(hp, num3, mbndry, box, a.d);
+    for (int q = 0; q < 2; q++) {
       l.ij = lists[q];
       l.count = counts[q];
+      l.serial = order.repeat[1 + q] ? 1 : 0;
       launch_bande_list(l, ctx->stream);   // the two lists run in order
     }
   }
@@ -958,7 +970,16 @@ int g3m3_bndry_inner(g3m3_ctx* ctx, float* const f[G3M3_NFIELDS], const float* p
   a.dy = (p->grd_ymax[mb - 1] - p->grd_ymin[mb - 1]) / ((float)p->ny - 1.0f);
   a.xmin = p->grd_xmin[mb - 1]; a.ymin = p->grd_ymin[mb - 1];
   a.re_equiv = p->re_equiv; a.v_rot = p->v_rot;
-  launch_bndry_inner(a, ctx->stream);
+  // the lists on the host, to find cells they name twice
+  const int* lp[3] = {ijsrf, ijmid, ijzero};
+  std::vector<int> hl[3];
+  const int* hp[3];
+  for (int q = 0; q < 3; q++) {
+    hl[q].resize((size_t)mb * 3 * a.num[q] + 1);
+    if (a.num[q] > 0 && (s = host_ints(ctx, lp[q], mb * 3 * a.num[q], hl[q].data()))) return s;
+    hp[q] = hl[q].data();
+  }
+  launch_bndry_inner(a, inner_order(hp, a.num, mb, mb, a.d), ctx->stream);
   return finish(ctx, "bndry_inner");
 }
 

@@ -137,6 +137,7 @@ void fields_stage(g3m3_model* m, Getter src, int b) {
     for (int q = 1; q < 3; q++) {
       l.ij = m->ij[q];
       l.count = m->num[q][b - 1];
+      l.serial = m->inner_order[b - 1].repeat[q] ? 1 : 0;
       launch_bande_list(l, S(m));
     }
     launch_bande_faces(ba.efld, m->d, S(m));
@@ -223,8 +224,7 @@ void inner_stage(g3m3_model* m, Getter target, cudaStream_t st) {
   a.dy = (p.grd_ymax[mb - 1] - p.grd_ymin[mb - 1]) / ((float)m->d.ny - 1.0f);
   a.xmin = p.grd_xmin[mb - 1]; a.ymin = p.grd_ymin[mb - 1];
   a.re_equiv = p.re_equiv; a.v_rot = p.v_rot;
-  launch_bndry_inner(a, st);
-  m->launches_in_step += 1;
+  m->launches_in_step += launch_bndry_inner(a, m->inner_order[mb - 1], st);
 }
 
 void boundary_stage(g3m3_model* m, Getter target, int b, int slot_t1, Getter inner_target = nullptr,
@@ -983,6 +983,12 @@ int g3m3_model_set_inner(g3m3_model* m, const float* resistive, const int* ijsrf
   if ((e = cudaMemcpy(rst.data(), resistive, rst.size() * sizeof(float), cudaMemcpyDefault)) != cudaSuccess)
     return cuda_check(m->ctx, e, "resistive");
   m->lists_unique = true;
+  for (int b = 1; b <= mb; b++) {
+    const int* hp[3] = {ij[0], ij[1], ij[2]};
+    const int nb[3] = {m->num[0][b - 1], m->num[1][b - 1], m->num[2][b - 1]};
+    m->inner_order[b - 1] = inner_order(hp, nb, mb, b, m->d);
+    if (m->inner_order[b - 1].any()) m->lists_unique = false;   // applied in the reference's order
+  }
   for (int b = 1; b <= mb; b++)
     for (int l = 1; l < 3; l++)
       for (int n = 0; n < m->num[l][b - 1]; n++) {

@@ -4,6 +4,9 @@
 //   flanks         sub_flanks.f90:5-303 (via sub_bndry_flanks.f90:105-209)
 //   corer          sub_corer.f90:5-55 (via sub_bndry_corer.f90:42-111)
 //   flanks_synced  sub_flanks_synced.f90:5-141
+#include <unordered_map>
+#include <unordered_set>
+
 #include "bndry.cuh"
 #include "launch.cuh"
 
@@ -172,13 +175,8 @@ __global__ void __launch_bounds__(256) k_bndry_outer(const __grid_constant__ Out
 }
 
 // ------------------------------------------------------------ bndry_inner
-__global__ void __launch_bounds__(128) k_bndry_inner(const __grid_constant__ InnerArgs a) {
-  int m = blockIdx.x * blockDim.x + threadIdx.x;
-  int l;
-  if (m < a.num[0]) l = 0;
-  else if ((m -= a.num[0]) < a.num[1]) l = 1;
-  else if ((m -= a.num[1]) < a.num[2]) l = 2;
-  else return;
+// entry m of list l (sub_bndry_inner.f90:81-265)
+__device__ void inner_entry(const InnerArgs& a, int l, int m) {
   const int* ij = a.ij[l];
   const float* parm = a.parm[l];
   const int mb = a.mbndry, b = a.box - 1;
@@ -216,6 +214,29 @@ __global__ void __launch_bounds__(128) k_bndry_inner(const __grid_constant__ Inn
   if (l == 2) {
     a.f[G3M3_F_BX][c] = 0.0f; a.f[G3M3_F_BY][c] = 0.0f; a.f[G3M3_F_BZ][c] = 0.0f;
   }
+}
+
+__global__ void __launch_bounds__(128) k_bndry_inner(const __grid_constant__ InnerArgs a) {
+  if (a.serial) {   // a list naming a cell twice: its entries in order
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+      for (int m = 0; m < a.num[a.only - 1]; m++) inner_entry(a, a.only - 1, m);
+    return;
+  }
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  int l;
+  if (a.only) {
+    l = a.only - 1;
+    if (m >= a.num[l]) return;
+  } else if (m < a.num[0]) {
+    l = 0;
+  } else if ((m -= a.num[0]) < a.num[1]) {
+    l = 1;
+  } else if ((m -= a.num[1]) < a.num[2]) {
+    l = 2;
+  } else {
+    return;
+  }
+  inner_entry(a, l, m);
 }
 
 // ------------------------------------------------------------ flanks
@@ -386,10 +407,43 @@ void launch_bndry_outer(const OuterArgs& a, cudaStream_t s) {
   k_bndry_outer<<<dim3((unsigned)((n + 255) / 256), G3M3_NFIELDS), 256, 0, s>>>(a);
 }
 
-void launch_bndry_inner(const InnerArgs& a, cudaStream_t s) {
-  const int n = a.num[0] + a.num[1] + a.num[2];
-  if (n <= 0) return;
-  k_bndry_inner<<<(n + 127) / 128, 128, 0, s>>>(a);
+int launch_bndry_inner(const InnerArgs& a, const InnerOrder& o, cudaStream_t s) {
+  if (!o.any()) {
+    const int n = a.num[0] + a.num[1] + a.num[2];
+    if (n <= 0) return 0;
+    k_bndry_inner<<<(n + 127) / 128, 128, 0, s>>>(a);
+    return 1;
+  }
+  int launches = 0;
+  for (int l = 0; l < 3; l++) {
+    if (a.num[l] <= 0) continue;
+    InnerArgs b = a;
+    b.only = l + 1;
+    b.serial = o.repeat[l] ? 1 : 0;
+    if (b.serial) k_bndry_inner<<<1, 1, 0, s>>>(b);
+    else k_bndry_inner<<<(a.num[l] + 127) / 128, 128, 0, s>>>(b);
+    launches += 1;
+  }
+  return launches;
+}
+
+InnerOrder inner_order(const int* const ij[3], const int num[3], int mbndry, int box, const Dims& d) {
+  InnerOrder o;
+  std::unordered_map<size_t, int> owner;   // cell -> the list that named it first
+  for (int l = 0; l < 3; l++) {
+    std::unordered_set<size_t> mine;
+    for (int n = 0; n < num[l]; n++) {
+      const int i = ij[l][(box - 1) + (size_t)mbndry * (0 + 3 * (size_t)n)];
+      const int j = ij[l][(box - 1) + (size_t)mbndry * (1 + 3 * (size_t)n)];
+      const int k = ij[l][(box - 1) + (size_t)mbndry * (2 + 3 * (size_t)n)];
+      if (i < 1 || j < 1 || k < 1 || i > d.nx || j > d.ny || k > d.nz) continue;
+      const size_t c = d.at(i, j, k);
+      if (!mine.insert(c).second) o.repeat[l] = true;
+      const auto it = owner.emplace(c, l).first;
+      if (it->second != l) o.overlap = true;
+    }
+  }
+  return o;
 }
 
 void launch_flanks(const FlanksArgs& a, cudaStream_t s) {

@@ -177,10 +177,8 @@ __global__ void __launch_bounds__(256) k_bande_interior(const __grid_constant__ 
   a.efld[2][c] = ez;
 }
 
-// One thread per list entry; entries of one list name distinct cells.
-__global__ void k_bande_list(const __grid_constant__ BandEListArgs a) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= a.count) return;
+// Entry m of a list: E += rst J / n at its cell (sub_BandE.f90:88-116).
+__device__ void bande_entry(const BandEListArgs& a, int m) {
   const int i = a.ij[(a.box - 1) + (size_t)a.mbndry * (0 + 3 * (size_t)m)];
   const int j = a.ij[(a.box - 1) + (size_t)a.mbndry * (1 + 3 * (size_t)m)];
   const int k = a.ij[(a.box - 1) + (size_t)a.mbndry * (2 + 3 * (size_t)m)];
@@ -192,6 +190,18 @@ __global__ void k_bande_list(const __grid_constant__ BandEListArgs a) {
   a.efld[0][c] = a.efld[0][c] + r * __ldg(a.cur[0] + c) / eden;
   a.efld[1][c] = a.efld[1][c] + r * __ldg(a.cur[1] + c) / eden;
   a.efld[2][c] = a.efld[2][c] + r * __ldg(a.cur[2] + c) / eden;
+}
+
+// One thread per entry when the list names each cell once; otherwise one
+// thread walks the list in order, as the reference does.
+__global__ void k_bande_list(const __grid_constant__ BandEListArgs a) {
+  if (a.serial) {
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+      for (int m = 0; m < a.count; m++) bande_entry(a, m);
+    return;
+  }
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m < a.count) bande_entry(a, m);
 }
 
 // Face copies of sub_BandE.f90:124-159: boundary = value at the clamped index.
@@ -271,7 +281,8 @@ void launch_bande_interior(const BandEArgs& a, cudaStream_t s) {
 
 void launch_bande_list(const BandEListArgs& a, cudaStream_t s) {
   if (a.count <= 0) return;
-  k_bande_list<<<blocks_for((size_t)a.count, 128), 128, 0, s>>>(a);
+  if (a.serial) k_bande_list<<<1, 1, 0, s>>>(a);
+  else k_bande_list<<<blocks_for((size_t)a.count, 128), 128, 0, s>>>(a);
 }
 
 void launch_bande_faces(float* const efld[3], const Dims& d, cudaStream_t s) {

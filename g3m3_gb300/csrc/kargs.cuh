@@ -88,6 +88,7 @@ struct BandEListArgs {     // the ijmid/ijzero resistive scatter
   int count, mbndry, box;
   Dims d;
   float rmass[3];
+  int serial;              // the list names a cell twice: one thread, in order
 };
 
 struct LapArgs {           // Lapidus smoothing of up to 10 fields with one velocity

@@ -7,6 +7,7 @@
 #include <string>
 #include <vector>
 
+#include "bndry.cuh"
 #include "ctx.cuh"
 
 namespace g3m3 {
@@ -38,6 +39,7 @@ struct g3m3_model {
   float* resistive = nullptr;
   float* rst_e = nullptr;            // BandE's resistive coefficient per cell (0: none)
   bool lists_unique = true;
+  g3m3::InnerOrder inner_order[G3M3_MAX_GRIDS];   // per box: how its inner-boundary lists must be applied
   int* ij[3] = {};
   float* parm[3] = {};
   int num[3][G3M3_MAX_GRIDS] = {};
