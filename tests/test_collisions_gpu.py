@@ -1,5 +1,5 @@
-"""Inner-boundary lists that name a cell twice (collisions), against the
-oracle, bitwise.  The reference applies its lists in turn (srf, mid,
+"""Inner-boundary lists that name a cell twice (collisions) or nothing
+(empty), against the oracle, bitwise.  The reference applies its lists in turn (srf, mid,
 zero), each entry in order, so a cell named twice ends with its last
 entry's values and BandE's resistive term adds once per entry.  The
 lists its own set-up builds never collide; these are the lists a caller
@@ -74,3 +74,32 @@ def test_engine_steps_with_colliding_lists(graph):
         m.close()
     for q in range(34):
         assert_same(g[q], om.cur[q], f"field {q}")
+
+
+@pytest.mark.parametrize("empty", ["srf", "mid", "zero", "all"])
+def test_bndry_inner_and_bande_empty_lists(empty):
+    """Lists with no entries (count 0) leave the fields to the other lists."""
+    I = Inputs("tiny2")
+    p = I.p
+    L = {k: v.copy() for k, v in I.lists.items()}
+    for name in (("srf", "mid", "zero") if empty == "all" else (empty,)):
+        L["num" + name][:] = 0
+    args = [list(I.wrk), L["parm_srf"], L["parm_mid"], L["parm_zero"], L["ijsrf"], L["numsrf"], L["ijmid"],
+            L["nummid"], L["ijzero"], L["numzero"], L["ijsrf"].shape[0], L["ijmid"].shape[0], L["ijzero"].shape[0],
+            p]
+    oa, ga = run_both("bndry_inner", args)
+    for q in range(34):
+        assert_same(ga[0][q], oa[0][q], f"bndry_inner field {q}")
+    box = 1
+    ef = I.scratch(1.0, 3)
+    bs = [(I.b0[q, box - 1] + I.cur[31 + q, box - 1]).astype(np.float32) for q in range(3)]
+    cur = I.scratch(0.1, 3)
+    ev = I.scratch(0.1, 3)
+    args = (ef + bs + cur + ev + [I.scratch(1.0)[0], I.cur[30], I.cur[0], I.cur[10], I.cur[20], I.resistive,
+                                  p.resist, p.reynolds]
+            + I.dims(box) + [p.rmassq, p.rmassh, p.rmasso, L["ijmid"], L["nummid"], L["ijzero"], p.mbndry,
+                             L["numzero"], L["ijmid"].shape[0], L["ijzero"].shape[0]]
+            + [float(p.xspac[box - 1])] * 3)
+    oa, ga = run_both("bande", args)
+    for k in range(3):
+        assert_same(ga[k], oa[k], f"BandE efld{k}")

@@ -342,6 +342,10 @@ def test_sample_points():
     gmin = np.array([[p.grd_xmin[b], p.grd_ymin[b], p.grd_zmin[b]] for b in range(p.n_grids)], np.float32)
     gmax = np.array([[p.grd_xmax[b], p.grd_ymax[b], p.grd_zmax[b]] for b in range(p.n_grids)], np.float32)
     xyz = (rng.uniform(-1, 1, (n, 3)) * np.array([20.0, 20.0, 8.0]) * p.re_equiv).astype(np.float32)
+    # points outside every box: findgrid clamps them into the outermost box
+    # (cft_findgrid.f90:49-54) and trilin_interp extrapolates from there
+    xyz[-6:] = (np.array([[500.0, 0, 0], [-500.0, 3, 1], [0, 400.0, 0], [2, -400.0, 1], [0, 1, 300.0],
+                          [-1, 0, -300.0]]) * p.re_equiv).astype(np.float32)
     xs = np.array(p.xspac[: p.n_grids], np.float32)
     field = I.cur[32]
     out = np.zeros(n, np.float32)
