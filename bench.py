@@ -210,9 +210,11 @@ def run_ours(args):
     m.state(out=host_np.reshape(34, p.n_grids, p.nz, p.ny, p.nx))
     # one call per main step: g3m3_model_step_host uploads each box on a copy
     # stream (the step waits for a box only before touching it), steps, and
-    # reads the state back.  Untimed warm-up first: the graphs captured for
-    # this host buffer (the buffer roles alternate between two schedules).
-    for _ in range(3):
+    # reads the state back.  Untimed warm-up first, one div B period of
+    # steps: the graphs of this host buffer for the schedule shapes a long
+    # run repeats (the buffer roles alternate; a shape first seen later is
+    # captured inside the window, about 23 ms once: e2e.ms_per_call).
+    for _ in range(10):
         m.step_host(host_np, host_np, graph=use_graph)
     # as many main steps as the device-timed region, so both hold the same
     # share of div B passes (one every 10th main step)
