@@ -251,6 +251,10 @@ class Model:
         self.ctx.check(self.L.g3m3_model_times(self.h, ctypes.byref(t), tsn, ctypes.byref(cu)))
         return t.value, np.array(tsn[:]), cu.value
 
+    def set_capture_after(self, n: int):
+        """Capture a step plan's graph at its n-th occurrence (1: at once)."""
+        self.ctx.check(self.L.g3m3_model_set_capture_after(self.h, int(n)))
+
     def clock(self):
         """(t, main steps done): the time and the count the div B cadence
         follows."""

@@ -1200,6 +1200,10 @@ int one_step(g3m3_model* m, int use_graph, std::vector<Action>& acts) {
     key += buf;
   }
   cudaError_t e;
+  // a plan seen fewer than capture_after times runs host-launched: a
+  // sub-cycling schedule that occurs once costs no capture
+  if (use_graph && m->capture_after > 1 && !m->graphs.count(key) && ++m->plan_seen[key] < m->capture_after)
+    use_graph = 0;
   if (use_graph) {
     cudaGraphExec_t ex = nullptr;
     if ((rc = step_graph(m, acts, key, &ex))) return rc;
@@ -1755,6 +1759,13 @@ int g3m3_model_times(g3m3_model* m, double* t, double* t_stepnew, int64_t* cell_
   if (t) *t = m->t;
   if (t_stepnew) std::memcpy(t_stepnew, m->t_stepnew, m->p.n_grids * sizeof(double));
   if (cell_updates) *cell_updates = m->cell_updates;
+  return G3M3_OK;
+}
+
+int g3m3_model_set_capture_after(g3m3_model* m, int n) {
+  if (!m || n < 1) return G3M3_ERR_ARG;
+  m->capture_after = n;
+  m->plan_seen.clear();
   return G3M3_OK;
 }
 

@@ -98,6 +98,8 @@ struct g3m3_model {
   int ncraft = 0, craft_nf = 0, craft_cap = 0, craft_t_slot = -1;
   int craft_fields[8] = {};
   std::map<std::string, cudaGraphExec_t> graphs;
+  std::map<std::string, int> plan_seen;   // host-launched sightings of a step plan not yet captured
+  int capture_after = 1;                  // capture a plan's graph at its n-th sighting
   std::map<std::string, int64_t> kernel_nodes;
   int64_t launches_in_step = 0;
   // adjoint recording (adjoint.cu): when set, every box-step, core sync

@@ -564,6 +564,12 @@ int g3m3_model_autotune(g3m3_model* m, int* fcs_variant);
 /* Time bookkeeping: t, t_stepnew(1..n_grids), executed cell-updates. */
 int g3m3_model_times(g3m3_model* m, double* t, double* t_stepnew,
     int64_t* cell_updates);
+/* Graph mode captures a main step's graph the first time its plan (the
+ * boxes' sub-cycling schedule and buffer roles) occurs, 20-30 ms once on the
+ * production grid.  With n > 1 a plan runs host-launched (about 3 % slower
+ * per step) until its n-th occurrence, so a schedule that occurs once in a
+ * long run is never captured.  Default 1. */
+int g3m3_model_set_capture_after(g3m3_model* m, int n);
 /* The model's clock: the simulation time t and the main steps done, whose
  * count sets the div B cadence (a pass after every divb_every-th main
  * step).  Restoring a clock read before a run repeats the run's schedule of

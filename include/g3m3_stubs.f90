@@ -1240,6 +1240,12 @@ module g3m3_c
       real(c_double) :: t_stepnew(*)
       integer(c_int64_t) :: cell_updates
     end function g3m3_model_times
+    function g3m3_model_set_capture_after(m, n) bind(C, name="g3m3_model_set_capture_after")
+      import
+      integer(c_int) :: g3m3_model_set_capture_after
+      type(c_ptr), value :: m
+      integer(c_int), value :: n
+    end function g3m3_model_set_capture_after
     function g3m3_model_get_clock(m, t, nsteps_done) bind(C, name="g3m3_model_get_clock")
       import
       integer(c_int) :: g3m3_model_get_clock

@@ -159,6 +159,29 @@ def test_ragged_grids_every_variant(limit, variant):
     assert cu == om.cell_updates
 
 
+def test_capture_after_second_occurrence():
+    """With g3m3_model_set_capture_after(2) a step plan runs host-launched
+    at its first occurrence and from a graph afterwards: the same bits."""
+    from oracle.oracle import OracleModel
+    from g3m3_gb300.api import Context, Model
+    st = make_config("tiny3")
+    om = OracleModel(st, omp=True)
+    om.init_steps()
+    for _ in range(6):
+        assert om.main_step() == 0
+    with Context() as ctx:
+        m = Model(ctx, st)
+        m.set_capture_after(2)
+        m.init_steps()
+        m.run(6, graph=True)
+        g = m.state()
+        k, gl = m.stats()
+        m.close()
+    assert 0 < gl < 6, gl
+    for q in range(34):
+        assert_same(g[q], om.cur[q], f"field {q}")
+
+
 @pytest.mark.parametrize("graph,pin", [(False, True), (True, True), (False, False)])
 def test_step_host(graph, pin):
     """Host-fed main steps (per-box uploads overlapping the step, result
